@@ -1,0 +1,165 @@
+/*
+ * ns_gpu.h -- C ABI of libns_gpu.so, the GB300 (sm_103a) FP64 staggered-grid
+ * incompressible Navier-Stokes step.
+ *
+ * This is the drop-in boundary for the time-step loop body of the reference
+ * (zzwz02/NS_3D_Staggered_dp):
+ *   big_periodic_3D.f90:326-571                       (periodic step)
+ *   re_simulation_sub_tstep_interBC_combine.f90:438-804 (sub-block step)
+ * and for the NS_functions.f90 / FD_functions.f90 routines it calls.  The
+ * Fortran drivers bind it through ISO_C_BINDING (include/ns_gpu.f90).
+ *
+ * Conventions
+ *  - All arrays crossing the boundary are FP64, column-major (Fortran order),
+ *    in the reference's exact padded shapes:
+ *        u (nx+1, ny+2, nz+2)   v (nx+2, ny+1, nz+2)   w (nx+2, ny+2, nz+1)
+ *        p (nx+2, ny+2, nz+2)   rhs_?_previous: same as u / v / w
+ *    Pointers are host pointers unless the name ends in _dev.
+ *  - Every call returns an int status (NS_OK = 0).  Nothing exits, aborts or
+ *    traps; ns_last_error() describes the last failure of a handle.
+ *  - One handle owns its device buffers and one CUDA stream.  A handle must
+ *    not be used by two host threads at once.  Host pointers are never
+ *    retained after a call returns.
+ *  - BC codes (NS_functions.f90:219-220): 1 periodic, 2 Dirichlet on the
+ *    wall (cell face), 3 Neumann on the wall, 4 Dirichlet on the ghost cell.
+ */
+#ifndef NS_GPU_H
+#define NS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum {
+  NS_OK = 0,
+  NS_ERR_SHAPE = 1,          /* unsupported / inconsistent grid size            */
+  NS_ERR_CUDA = 2,           /* a CUDA runtime call failed                      */
+  NS_ERR_NONFINITE = 3,      /* NaN/Inf found by a checked call                 */
+  NS_ERR_TIMEOUT = 4,        /* a bounded device wait ran out                   */
+  NS_ERR_UNSUPPORTED_BC = 5, /* bc/pbc/scheme combination the step cannot run   */
+  NS_ERR_ARG = 6,            /* NULL or out-of-range argument                   */
+  NS_ERR_NOMEM = 7           /* device allocation failed                        */
+};
+
+/* Time schemes (big_periodic_3D.f90:350-490). */
+enum { NS_EULER = 0, NS_AB2 = 1, NS_AB2_CN = 2 };
+
+/* Boundary-condition codes. */
+enum { NS_BC_PERIODIC = 1, NS_BC_DIRICHLET = 2, NS_BC_NEUMANN = 3, NS_BC_GHOST = 4 };
+
+/*
+ * Step configuration: the compile-time parameters of the reference drivers
+ * (big_periodic_3D.f90:9-13,104-108; re_simulation_sub_tstep_interBC_combine.f90:100-112).
+ */
+typedef struct ns_config {
+  int nx, ny, nz;       /* interior cells per axis                                 */
+  double lx, ly, lz;    /* domain lengths; dx = lx/nx etc.                         */
+  double nu;            /* kinematic viscosity                                     */
+  double dt;            /* time step (dt0)                                         */
+  int scheme;           /* NS_EULER, NS_AB2, NS_AB2_CN                             */
+  int bc[3];            /* velocity BC per axis: 1, 2 or 4                         */
+  int pbc[3];           /* pressure BC per axis: 1, 2, 3 or 4                      */
+  int dp_flag;          /* 0: p = dp; 1: incremental (p += dp, -dt*grad p in u*)   */
+  int gauge;            /* 1: dp -= dp(1,1,1) after the solve (big_periodic_3D.f90:562) */
+  double mean_dp;       /* mean imposed on the singular mode (NS_functions.f90:1576) */
+  int cn_periodic_closure; /* 0: reference closure of the periodic normal-component
+                              CN row, A(1,n+1) (NS_functions.f90:1273); 1: A(1,n)   */
+  int use_graph;        /* 1: replay each step from a captured CUDA graph          */
+  int reserved[8];
+} ns_config;
+
+/* Diagnostics (big_periodic_3D.f90:572-579). */
+typedef struct ns_diag {
+  double max_div;          /* max |div u| over the interior                       */
+  double probe;            /* u(nx/2, ny/2, nz/2) (Fortran indices)                */
+  long long steps_done;    /* steps taken since ns_set_state                       */
+  int euler_start_pending; /* 1 if the next step is the Euler start of AB2/AB2-CN  */
+  int reserved;
+} ns_diag;
+
+typedef struct ns_handle ns_handle;
+
+/* ------------------------------------------------------------------------
+ * Session tier: state resident on the GPU between steps.
+ * ------------------------------------------------------------------------ */
+
+/* Fill *cfg with the big_periodic_3D defaults for an nx*ny*nz periodic box on
+ * [0,2pi]^3 (big_periodic_3D.f90:10-13,104-108). */
+int ns_config_default(ns_config* cfg, int nx, int ny, int nz);
+
+/* Create a session: device buffers, stream, CN factors, transform plans.
+ * Replaces the driver set-up of big_periodic_3D.f90:158-256 and
+ * re_simulation_sub_tstep_interBC_combine.f90:200-354. */
+int ns_create(const ns_config* cfg, ns_handle** out);
+int ns_destroy(ns_handle* h);
+const char* ns_last_error(const ns_handle* h);
+const char* ns_status_string(int status);
+
+/* Use an external CUDA stream (cudaStream_t) instead of the handle's own. */
+int ns_set_stream(ns_handle* h, void* cuda_stream);
+int ns_synchronize(ns_handle* h);
+
+/* Copy the state in.  u, v, w, p are required; the three rhs_?_previous may be
+ * NULL, in which case the AB2 history is zero and the next step is the Euler
+ * start (big_periodic_3D.f90:296-303 init read, :309-324 restart read). */
+int ns_set_state(ns_handle* h, const double* u, const double* v, const double* w, const double* p,
+                 const double* rhs_x_prev, const double* rhs_y_prev, const double* rhs_z_prev);
+
+/* Copy the state out (any pointer may be NULL to skip that field).  History
+ * entries outside the interior ranges are returned as zero. */
+int ns_get_state(ns_handle* h, double* u, double* v, double* w, double* p,
+                 double* rhs_x_prev, double* rhs_y_prev, double* rhs_z_prev);
+
+/* Boundary faces, in the reference shapes and order of get_velpr_bc's
+ * outputs (NS_functions.f90:414-420):
+ *   bx_u_1, bx_u_nx, by_u_1, by_u_ny, bz_u_1, bz_u_nz,
+ *   bx_v_1, bx_v_nx, by_v_1, by_v_ny, bz_v_1, bz_v_nz,
+ *   bx_w_1, bx_w_nx, by_w_1, by_w_ny, bz_w_1, bz_w_nz,
+ *   bx_p_1, bx_p_nx, by_p_1, by_p_ny, bz_p_1, bz_p_nz.
+ * set == 0: the faces used by vel_bc_staggered and the pressure BC;
+ * set == 1, 2, 3: the faces of the x, y, z AB2-CN sweep
+ * (vel_bc_staggered_CN2, big_periodic_3D.f90:425,437,462).  A NULL entry
+ * means zero.  Faces persist until set again. */
+int ns_set_faces(ns_handle* h, int set, const double* const faces[24]);
+
+/* Advance nsteps steps (the loop body of big_periodic_3D.f90:326-567). */
+int ns_step(ns_handle* h, int nsteps);
+
+/* max|div u| and the probe value of the current state (a synchronous call). */
+int ns_get_diag(ns_handle* h, ns_diag* d);
+
+/* ------------------------------------------------------------------------
+ * Routine tier: one reference routine per call, host arrays in and out,
+ * using the handle's configuration for shapes, bc codes and spacings.
+ * ------------------------------------------------------------------------ */
+
+/* cal_conv (NS_functions.f90:53-158): conv_? in the reference's shapes
+ * ((nx or nx-1), ny, nz) etc. per bc. */
+int ns_cal_conv(ns_handle* h, const double* u, const double* v, const double* w,
+                double* conv_x, double* conv_y, double* conv_z);
+
+/* cal_diff (NS_functions.f90:161-210): Laplacian, same shapes as cal_conv. */
+int ns_cal_diff(ns_handle* h, const double* u, const double* v, const double* w,
+                double* diff_x, double* diff_y, double* diff_z);
+
+/* Pressure Poisson solve: rhs (nx, ny, nz), already BC-modified as by
+ * pr_bc_staggered_modify_rhs, -> dp (nx+2, ny+2, nz+2) with ghosts filled by
+ * pr_bc_staggered using the set-0 faces.  FFT for all-periodic pbc
+ * (big_periodic_3D.f90:526-543), DCT/DST otherwise (NS_functions.f90:1505-1630). */
+int ns_poisson(ns_handle* h, const double* rhs, double* dp);
+
+/* The three AB2-CN ADI sweeps on u*, v*, w* in place, with the set-1..3 faces
+ * (big_periodic_3D.f90:425-489; re_simulation_sub_tstep_interBC_combine.f90:656-701). */
+int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star);
+
+/* Version string of the library build. */
+const char* ns_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NS_GPU_H */

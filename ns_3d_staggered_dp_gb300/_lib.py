@@ -1,0 +1,80 @@
+"""ctypes binding of libns_gpu.so (the C ABI declared in include/ns_gpu.h).
+
+There is no CPU fallback: if the library is missing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libns_gpu.so")
+
+NS_OK = 0
+STATUS = {0: "NS_OK", 1: "NS_ERR_SHAPE", 2: "NS_ERR_CUDA", 3: "NS_ERR_NONFINITE", 4: "NS_ERR_TIMEOUT",
+          5: "NS_ERR_UNSUPPORTED_BC", 6: "NS_ERR_ARG", 7: "NS_ERR_NOMEM"}
+
+
+class NSConfig(C.Structure):
+    """Mirror of ``ns_config`` (include/ns_gpu.h)."""
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
+        ("nu", C.c_double), ("dt", C.c_double),
+        ("scheme", C.c_int),
+        ("bc", C.c_int * 3), ("pbc", C.c_int * 3),
+        ("dp_flag", C.c_int), ("gauge", C.c_int),
+        ("mean_dp", C.c_double),
+        ("cn_periodic_closure", C.c_int),
+        ("use_graph", C.c_int),
+        ("reserved", C.c_int * 8),
+    ]
+
+
+class NSDiag(C.Structure):
+    _fields_ = [("max_div", C.c_double), ("probe", C.c_double), ("steps_done", C.c_longlong),
+                ("euler_start_pending", C.c_int), ("reserved", C.c_int)]
+
+
+# Every entry point of include/ns_gpu.h with its ctypes signature.
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "ns_config_default": (C.c_int, [C.POINTER(NSConfig), C.c_int, C.c_int, C.c_int]),
+    "ns_create": (C.c_int, [C.POINTER(NSConfig), C.POINTER(C.c_void_p)]),
+    "ns_destroy": (C.c_int, [C.c_void_p]),
+    "ns_last_error": (C.c_char_p, [C.c_void_p]),
+    "ns_status_string": (C.c_char_p, [C.c_int]),
+    "ns_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ns_synchronize": (C.c_int, [C.c_void_p]),
+    "ns_set_state": (C.c_int, [C.c_void_p] + [_DP] * 7),
+    "ns_get_state": (C.c_int, [C.c_void_p] + [_DP] * 7),
+    "ns_set_faces": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_DP)]),
+    "ns_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ns_get_diag": (C.c_int, [C.c_void_p, C.POINTER(NSDiag)]),
+    "ns_cal_conv": (C.c_int, [C.c_void_p] + [_DP] * 6),
+    "ns_cal_diff": (C.c_int, [C.c_void_p] + [_DP] * 6),
+    "ns_poisson": (C.c_int, [C.c_void_p, _DP, _DP]),
+    "ns_adi": (C.c_int, [C.c_void_p, _DP, _DP, _DP]),
+    "ns_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libns_gpu.so (build it first with ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libns_gpu.so not found at {p}: build it with "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib

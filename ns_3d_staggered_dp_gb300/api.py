@@ -1,0 +1,188 @@
+"""Host-side mirror of the reference's step interface over the C ABI.
+
+The Fortran drivers of the reference (big_periodic_3D.f90,
+re_simulation*.f90) call NS_functions.f90 routines on column-major padded
+arrays.  ``Session`` replaces the time-loop body with GPU-resident state;
+the module-level functions replace single routines.  Arrays are NumPy
+float64 in the reference's shapes; they are passed to the library in
+Fortran order.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+
+EULER, AB2, AB2_CN = 0, 1, 2
+PI = 3.1415926535897932
+
+FACE_ORDER = [  # get_velpr_bc output order (NS_functions.f90:414-420)
+    "x_u_1", "x_u_n", "y_u_1", "y_u_n", "z_u_1", "z_u_n",
+    "x_v_1", "x_v_n", "y_v_1", "y_v_n", "z_v_1", "z_v_n",
+    "x_w_1", "x_w_n", "y_w_1", "y_w_n", "z_w_1", "z_w_n",
+    "x_p_1", "x_p_n", "y_p_1", "y_p_n", "z_p_1", "z_p_n",
+]
+
+
+class NSError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_lib.STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _f(a, shape=None):
+    a = np.asarray(a, dtype=np.float64)
+    if shape is not None and tuple(a.shape) != tuple(shape):
+        raise NSError(1, f"shape {a.shape} != {shape}")
+    return np.asfortranarray(a)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def shapes(nx, ny, nz):
+    return {"u": (nx + 1, ny + 2, nz + 2), "v": (nx + 2, ny + 1, nz + 2), "w": (nx + 2, ny + 2, nz + 1),
+            "p": (nx + 2, ny + 2, nz + 2)}
+
+
+def make_config(nx, ny, nz, **kw) -> _lib.NSConfig:
+    """ns_config with the big_periodic_3D defaults, overridden by keywords
+    (bc/pbc take 3-tuples)."""
+    lib = _lib.load()
+    c = _lib.NSConfig()
+    lib.ns_config_default(C.byref(c), nx, ny, nz)
+    for k, v in kw.items():
+        if k in ("bc", "pbc"):
+            for i in range(3):
+                getattr(c, k)[i] = int(v[i])
+        else:
+            setattr(c, k, v)
+    return c
+
+
+class Session:
+    """One GPU-resident simulation (ns_create / ns_step / ns_destroy)."""
+
+    def __init__(self, cfg=None, **kw):
+        self.lib = _lib.load()
+        if cfg is None:
+            cfg = make_config(kw.pop("nx"), kw.pop("ny"), kw.pop("nz"), **kw)
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        s = self.lib.ns_create(C.byref(cfg), C.byref(self.h))
+        if s != 0:
+            raise NSError(s, "ns_create failed")
+        self.shapes = shapes(cfg.nx, cfg.ny, cfg.nz)
+
+    def _check(self, s):
+        if s != 0:
+            raise NSError(s, self.lib.ns_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.ns_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, u, v, w, p, rhs_prev=None):
+        sh = self.shapes
+        u, v, w, p = _f(u, sh["u"]), _f(v, sh["v"]), _f(w, sh["w"]), _f(p, sh["p"])
+        if rhs_prev is None:
+            hx = hy = hz = None
+        else:
+            hx, hy, hz = _f(rhs_prev[0], sh["u"]), _f(rhs_prev[1], sh["v"]), _f(rhs_prev[2], sh["w"])
+        self._keep = (u, v, w, p, hx, hy, hz)
+        self._check(self.lib.ns_set_state(self.h, _ptr(u), _ptr(v), _ptr(w), _ptr(p), _ptr(hx), _ptr(hy), _ptr(hz)))
+
+    def get_state(self, history=True):
+        sh = self.shapes
+        out = {k: np.zeros(sh[k], order="F") for k in ("u", "v", "w", "p")}
+        hist = [np.zeros(sh[k], order="F") for k in ("u", "v", "w")] if history else [None] * 3
+        self._check(self.lib.ns_get_state(self.h, _ptr(out["u"]), _ptr(out["v"]), _ptr(out["w"]), _ptr(out["p"]),
+                                          _ptr(hist[0]), _ptr(hist[1]), _ptr(hist[2])))
+        if history:
+            out["hx"], out["hy"], out["hz"] = hist
+        return out
+
+    def set_faces(self, faces: dict, which=0):
+        """faces: {name: 2D array} using FACE_ORDER names; missing = zero."""
+        keep = []
+        arr = (C.POINTER(C.c_double) * 24)()
+        for i, k in enumerate(FACE_ORDER):
+            if k in faces and faces[k] is not None:
+                a = _f(faces[k])
+                keep.append(a)
+                arr[i] = _ptr(a)
+            else:
+                arr[i] = None
+        self._check(self.lib.ns_set_faces(self.h, which, arr))
+
+    def step(self, n=1):
+        self._check(self.lib.ns_step(self.h, n))
+
+    def synchronize(self):
+        self._check(self.lib.ns_synchronize(self.h))
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.lib.ns_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def diag(self):
+        d = _lib.NSDiag()
+        self._check(self.lib.ns_get_diag(self.h, C.byref(d)))
+        return {"max_div": d.max_div, "probe": d.probe, "steps": d.steps_done,
+                "euler_start_pending": bool(d.euler_start_pending)}
+
+    # routine tier -----------------------------------------------------------
+    def _conv_shapes(self):
+        c = self.cfg
+        sx = (c.nx if c.bc[0] == 1 else c.nx - 1, c.ny, c.nz)
+        sy = (c.nx, c.ny if c.bc[1] == 1 else c.ny - 1, c.nz)
+        sz = (c.nx, c.ny, c.nz if c.bc[2] == 1 else c.nz - 1)
+        return sx, sy, sz
+
+    def cal_conv(self, u, v, w):
+        """cal_conv (NS_functions.f90:53-158)."""
+        sh = self.shapes
+        u, v, w = _f(u, sh["u"]), _f(v, sh["v"]), _f(w, sh["w"])
+        outs = [np.zeros(s, order="F") for s in self._conv_shapes()]
+        self._check(self.lib.ns_cal_conv(self.h, _ptr(u), _ptr(v), _ptr(w), *[_ptr(o) for o in outs]))
+        return tuple(outs)
+
+    def cal_diff(self, u, v, w):
+        """cal_diff (NS_functions.f90:161-210)."""
+        sh = self.shapes
+        u, v, w = _f(u, sh["u"]), _f(v, sh["v"]), _f(w, sh["w"])
+        outs = [np.zeros(s, order="F") for s in self._conv_shapes()]
+        self._check(self.lib.ns_cal_diff(self.h, _ptr(u), _ptr(v), _ptr(w), *[_ptr(o) for o in outs]))
+        return tuple(outs)
+
+    def poisson(self, rhs):
+        """Poisson solve of a BC-modified RHS (nx, ny, nz) -> dp with ghosts."""
+        c = self.cfg
+        r = _f(rhs, (c.nx, c.ny, c.nz))
+        dp = np.zeros(self.shapes["p"], order="F")
+        self._check(self.lib.ns_poisson(self.h, _ptr(r), _ptr(dp)))
+        return dp
+
+    def adi(self, us, vs, ws):
+        """The three CN-ADI sweeps on u*, v*, w* (returns new arrays)."""
+        sh = self.shapes
+        us, vs, ws = (np.array(_f(us, sh["u"]), order="F"), np.array(_f(vs, sh["v"]), order="F"),
+                      np.array(_f(ws, sh["w"]), order="F"))
+        self._check(self.lib.ns_adi(self.h, _ptr(us), _ptr(vs), _ptr(ws)))
+        return us, vs, ws

@@ -1,0 +1,753 @@
+// C ABI of libns_gpu.so: sessions, state transfer, boundary faces, the time
+// step and the routine tier.  See include/ns_gpu.h for the contract and the
+// reference routine each entry point replaces.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ns_internal.cuh"
+#include "ns_kernels.cuh"
+
+namespace ns {
+bool fft_size_supported(int nx, int ny, int nz);
+}
+
+using namespace ns;
+
+namespace {
+
+// Host description of one tridiagonal line system of an ADI sweep.
+struct HostLineSys {
+  std::vector<double> l, dinv, cu, z;
+  double s0 = 0, s1 = 0;
+  int zA = 0, zB = 0, lo = 0, hi = 0, periodic = 0, n = 0;
+};
+
+// LU factors (no pivoting) of tridiag(a, b, c), a[0] and c[m-1] unused.
+void thomas_factor(const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& c,
+                   HostLineSys& S) {
+  const int m = (int)b.size();
+  S.l.assign(m, 0.0); S.dinv.assign(m, 0.0); S.cu.assign(m, 0.0);
+  double d = b[0];
+  S.dinv[0] = 1.0 / d;
+  S.cu[0] = m > 1 ? c[0] / d : 0.0;
+  for (int i = 1; i < m; ++i) {
+    S.l[i] = a[i] / d;
+    d = b[i] - S.l[i] * c[i - 1];
+    S.dinv[i] = 1.0 / d;
+    S.cu[i] = (i + 1 < m) ? c[i] / d : 0.0;
+  }
+}
+
+std::vector<double> thomas_solve(const HostLineSys& S, std::vector<double> r) {
+  const int m = (int)r.size();
+  for (int i = 1; i < m; ++i) r[i] -= S.l[i] * r[i - 1];
+  r[m - 1] *= S.dinv[m - 1];
+  for (int i = m - 2; i >= 0; --i) r[i] = r[i] * S.dinv[i] - S.cu[i] * r[i + 1];
+  return r;
+}
+
+// CN system of one sweep axis (mat_CN, NS_functions.f90:1245-1294).
+// normal: the swept field is staggered along the axis (A matrix, n+1
+// unknowns); otherwise tangential (B matrix, n+2 unknowns).
+HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool normal, int closure) {
+  const double idx2 = 1.0 / (h * h);
+  const double dg = 1.0 + 0.5 * dt * nu * 2.0 * idx2;
+  const double of = -0.5 * dt * nu * 1.0 * idx2;
+  HostLineSys S;
+  S.n = n;
+  if (bc == 1) {
+    // Reduced cyclic system on slots 1..n.
+    std::vector<double> a(n, of), b(n, dg), c(n, of);
+    double tr = of, bl = of;  // M[0][n-1], M[n-1][0]
+    if (normal && closure == 0) {
+      // A(1,n+1) ties face 1 to the duplicate face n+1 = face 1 (reference closure)
+      b[0] = dg + of;
+      tr = 0.0;
+    }
+    const double gam = -b[0];
+    b[0] -= gam;
+    b[n - 1] -= tr * bl / gam;
+    HostLineSys T;
+    thomas_factor(a, b, c, T);
+    std::vector<double> u(n, 0.0);
+    u[0] = gam;
+    u[n - 1] += bl;
+    std::vector<double> z = thomas_solve(T, u);
+    const double vlast = tr / gam;
+    const double fac = 1.0 + z[0] + vlast * z[n - 1];
+    S.l = T.l; S.dinv = T.dinv; S.cu = T.cu; S.z = z;
+    S.s0 = 1.0 / fac;
+    S.s1 = vlast / fac;
+    double zmax = 0;
+    for (double q : z) zmax = std::fmax(zmax, std::fabs(q));
+    const double thr = 1e-18 * zmax;
+    int zA = 0, zB = n;
+    for (int i = 0; i < n / 2; ++i)
+      if (std::fabs(z[i]) >= thr) zA = i + 1;
+    for (int i = n - 1; i >= n / 2; --i)
+      if (std::fabs(z[i]) >= thr) zB = i;
+    S.zA = zA; S.zB = zB;
+    S.lo = 1; S.hi = n; S.periodic = 1;
+    return S;
+  }
+  const int m = normal ? n + 1 : n + 2;
+  std::vector<double> a(m, of), b(m, dg), c(m, of);
+  if (normal) {  // rows 1 and n+1: identity (bc 2 and 4)
+    b[0] = 1.0; c[0] = 0.0;
+    b[m - 1] = 1.0; a[m - 1] = 0.0;
+    S.lo = 1; S.hi = n + 1;
+  } else {
+    if (bc == 2) {
+      b[0] = 0.5; c[0] = 0.5;
+      b[m - 1] = 0.5; a[m - 1] = 0.5;
+    } else {
+      b[0] = 1.0; c[0] = 0.0;
+      b[m - 1] = 1.0; a[m - 1] = 0.0;
+    }
+    S.lo = 0; S.hi = n + 1;
+  }
+  a[0] = 0.0; c[m - 1] = 0.0;
+  thomas_factor(a, b, c, S);
+  S.periodic = 0;
+  S.z.assign(1, 0.0);
+  return S;
+}
+
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The handle
+// ---------------------------------------------------------------------------
+struct ns_handle {
+  ns_config cfg;
+  Layout L;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  double dx, dy, dz;
+  // device fields
+  double *u = nullptr, *v = nullptr, *w = nullptr, *p = nullptr;
+  double *hx = nullptr, *hy = nullptr, *hz = nullptr;
+  double *us = nullptr, *vs = nullptr, *ws = nullptr, *dp = nullptr;
+  double2* spec = nullptr;
+  double* inv_lam = nullptr;
+  double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
+  FftPlan plan{};
+  // ADI factors
+  double* adi_buf = nullptr;
+  LineSys sys[3][3];  // [axis][field]
+  // faces: [set 0..3][axis][field 0..3][side] -> device planes
+  double* face_buf = nullptr;
+  FaceSet faces[4]{};
+  bool face_set_nonzero[4] = {false, false, false, false};
+  unsigned long long* diag_bits = nullptr;
+  // state
+  bool first_pending = true;
+  long long steps = 0;
+  std::string err;
+  // graphs
+  cudaGraphExec_t graph = nullptr;
+  bool eager_done = false;
+};
+
+namespace {
+
+int fail(ns_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define NS_CUDA(h, call)                                                                     \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail((h), NS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+// Internal slot offset per field and axis: face axis -> 0, cell axis -> -1.
+// field 0 u (face x), 1 v (face y), 2 w (face z), 3 p (cells).
+inline int slot_off(int field, int axis) { return (field == axis) ? 0 : -1; }
+// Reference extent of a field along an axis.
+inline int ext_of(const ns_config& c, int field, int axis) {
+  const int n = axis == 0 ? c.nx : (axis == 1 ? c.ny : c.nz);
+  return (field == axis) ? n + 1 : n + 2;
+}
+
+// Copy a Fortran array (reference shape) into the padded device field.
+cudaError_t h2d_field(ns_handle* h, double* dst, const double* src, int field) {
+  const ns_config& c = h->cfg;
+  const int ex = ext_of(c, field, 0), ey = ext_of(c, field, 1), ez = ext_of(c, field, 2);
+  cudaMemcpy3DParms prm{};
+  prm.srcPtr = make_cudaPitchedPtr((void*)src, ex * sizeof(double), ex, ey);
+  prm.dstPtr = make_cudaPitchedPtr((void*)(dst + h->L.off), h->L.px * sizeof(double), h->L.px, c.ny + 2);
+  prm.dstPos = make_cudaPos((1 + slot_off(field, 0)) * sizeof(double), 1 + slot_off(field, 1), 1 + slot_off(field, 2));
+  prm.extent = make_cudaExtent(ex * sizeof(double), ey, ez);
+  prm.kind = cudaMemcpyHostToDevice;
+  return cudaMemcpy3DAsync(&prm, h->stream);
+}
+
+cudaError_t d2h_field(ns_handle* h, double* dst, const double* src, int field) {
+  const ns_config& c = h->cfg;
+  const int ex = ext_of(c, field, 0), ey = ext_of(c, field, 1), ez = ext_of(c, field, 2);
+  cudaMemcpy3DParms prm{};
+  prm.srcPtr = make_cudaPitchedPtr((void*)(src + h->L.off), h->L.px * sizeof(double), h->L.px, c.ny + 2);
+  prm.srcPos = make_cudaPos((1 + slot_off(field, 0)) * sizeof(double), 1 + slot_off(field, 1), 1 + slot_off(field, 2));
+  prm.dstPtr = make_cudaPitchedPtr((void*)dst, ex * sizeof(double), ex, ey);
+  prm.extent = make_cudaExtent(ex * sizeof(double), ey, ez);
+  prm.kind = cudaMemcpyDeviceToHost;
+  return cudaMemcpy3DAsync(&prm, h->stream);
+}
+
+// Plane size of face planes for an axis (full box extent of the two other axes).
+inline int plane_n1(const Layout& L, int axis) { return axis == 0 ? L.ny + 2 : L.nx + 2; }
+inline int plane_n2(const Layout& L, int axis) { return axis == 2 ? L.ny + 2 : L.nz + 2; }
+inline size_t plane_size(const Layout& L, int axis) { return (size_t)plane_n1(L, axis) * plane_n2(L, axis); }
+
+// Offsets of a face plane inside face_buf.
+size_t face_offset(const Layout& L, int set, int axis, int field, int side) {
+  size_t off = 0;
+  for (int s = 0; s < 4; ++s)
+    for (int a = 0; a < 3; ++a)
+      for (int f = 0; f < 4; ++f)
+        for (int d = 0; d < 2; ++d) {
+          if (s == set && a == axis && f == field && d == side) return off;
+          off += plane_size(L, a);
+        }
+  return off;
+}
+size_t face_total(const Layout& L) {
+  size_t t = 0;
+  for (int a = 0; a < 3; ++a) t += 4 * 8 * plane_size(L, a);
+  return t;
+}
+
+// Convert one reference face array (2D, Fortran order over the two other
+// axes of the field) into a device plane in internal slot order.
+void face_to_plane(const ns_config& c, const Layout& L, int axis, int field, const double* src, double* plane) {
+  const int a1 = axis == 0 ? 1 : 0;
+  const int a2 = axis == 2 ? 1 : 2;
+  const int e1 = ext_of(c, field, a1), e2 = ext_of(c, field, a2);
+  const int o1 = 1 + slot_off(field, a1), o2 = 1 + slot_off(field, a2);
+  const int n1 = plane_n1(L, axis);
+  for (int q = 0; q < e2; ++q)
+    for (int r = 0; r < e1; ++r) plane[(size_t)(r + o1) + (size_t)n1 * (q + o2)] = src[r + (size_t)e1 * q];
+}
+
+int validate(const ns_config& c, std::string& msg) {
+  if (c.nx < 4 || c.ny < 4 || c.nz < 4) { msg = "grid too small"; return NS_ERR_SHAPE; }
+  if (c.scheme < 0 || c.scheme > 2) { msg = "scheme must be 0 (Euler), 1 (AB2) or 2 (AB2-CN)"; return NS_ERR_ARG; }
+  for (int a = 0; a < 3; ++a) {
+    if (c.bc[a] != 1 && c.bc[a] != 2 && c.bc[a] != 4) {
+      msg = "velocity bc must be 1, 2 or 4 (3 leaves the ghosts undefined in the reference)";
+      return NS_ERR_UNSUPPORTED_BC;
+    }
+    if (c.pbc[a] < 1 || c.pbc[a] > 4) { msg = "pbc must be 1..4"; return NS_ERR_UNSUPPORTED_BC; }
+    if ((c.bc[a] == 1) != (c.pbc[a] == 1)) { msg = "bc and pbc must agree on periodicity"; return NS_ERR_UNSUPPORTED_BC; }
+  }
+  const bool allper = c.pbc[0] == 1 && c.pbc[1] == 1 && c.pbc[2] == 1;
+  if (!allper) { msg = "non-periodic pressure BCs need the DCT solver, not in this build"; return NS_ERR_UNSUPPORTED_BC; }
+  if (!ns::fft_size_supported(c.nx, c.ny, c.nz)) {
+    msg = "FFT sizes must be powers of two in [16, 512]";
+    return NS_ERR_SHAPE;
+  }
+  if (!(c.dt > 0) || !(c.nu >= 0) || !(c.lx > 0) || !(c.ly > 0) || !(c.lz > 0)) { msg = "dt, nu, lengths"; return NS_ERR_ARG; }
+  return NS_OK;
+}
+
+PredictArgs predict_args(ns_handle* h) {
+  const ns_config& c = h->cfg;
+  PredictArgs a{};
+  a.L = h->L;
+  a.u = h->u; a.v = h->v; a.w = h->w; a.p = h->p;
+  a.us = h->us; a.vs = h->vs; a.ws = h->ws;
+  a.hx = h->hx; a.hy = h->hy; a.hz = h->hz;
+  a.one = 1.0; a.mzero = -0.0;
+  a.ulo = c.bc[0] == 1 ? 1 : 2;
+  a.vlo = c.bc[1] == 1 ? 1 : 2;
+  a.wlo = c.bc[2] == 1 ? 1 : 2;
+  const double dx = h->dx, dy = h->dy, dz = h->dz, dt = c.dt, nu = c.nu;
+  a.cx = -0.25 / dx; a.cy = -0.25 / dy; a.cz = -0.25 / dz;
+  const double ix2 = 1.0 / (dx * dx), iy2 = 1.0 / (dy * dy), iz2 = 1.0 / (dz * dz);
+  a.kx = nu * ix2; a.ky = nu * iy2; a.kz = nu * iz2;
+  a.k0 = -2.0 * nu * (ix2 + iy2 + iz2);
+  const double hnd = 0.5 * nu * dt;
+  a.ca = hnd * ix2; a.cb = hnd * iy2; a.cc = hnd * iz2;
+  a.c0 = 1.0 - 2.0 * hnd * (ix2 + iy2 + iz2);
+  a.cC = 1.5 * dt; a.cP = -0.5 * dt;
+  a.dt = dt; a.e1 = 1.5 * dt; a.e2 = -0.5 * dt;
+  a.gpx = -dt / dx; a.gpy = -dt / dy; a.gpz = -dt / dz;
+  a.ix2 = ix2; a.iy2 = iy2; a.iz2 = iz2; a.lap0 = -2.0 * (ix2 + iy2 + iz2);
+  return a;
+}
+
+int enqueue_adi(ns_handle* h) {
+  const ns_config& c = h->cfg;
+  for (int ax = 0; ax < 3; ++ax) {
+    AdiArgs a{};
+    a.L = h->L;
+    a.f[0] = h->us; a.f[1] = h->vs; a.f[2] = h->ws;
+    for (int f = 0; f < 3; ++f) {
+      a.sys[f] = h->sys[ax][f];
+      a.face_lo[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][0] : nullptr;
+      a.face_hi[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][1] : nullptr;
+      const int n1 = plane_n1(h->L, ax), n2 = plane_n2(h->L, ax);
+      a.ext_lo[f][0] = 0; a.ext_lo[f][1] = 0;
+      a.ext_hi[f][0] = n1 - 1; a.ext_hi[f][1] = n2 - 1;
+    }
+    (void)c;
+    NS_CUDA(h, launch_adi(ax, a, h->stream));
+  }
+  return NS_OK;
+}
+
+int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
+  const ns_config& c = h->cfg;
+  DivArgs d{};
+  d.rhs = rhs;
+  d.L = h->L;
+  d.us = h->us; d.vs = h->vs; d.ws = h->ws;
+  d.cdx = 1.0 / (h->dx * c.dt); d.cdy = 1.0 / (h->dy * c.dt); d.cdz = 1.0 / (h->dz * c.dt);
+  d.one = 1.0; d.mzero = -0.0;
+  NS_CUDA(h, launch_fft_poisson(h->plan, d, h->spec, nullptr, h->dp, h->L, h->stream));
+  NS_CUDA(h, launch_pr_bc(h->L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, h->dz, h->stream));
+  return NS_OK;
+}
+
+int enqueue_step(ns_handle* h, bool first) {
+  const ns_config& c = h->cfg;
+  PredictArgs a = predict_args(h);
+  NS_CUDA(h, launch_predict(a, c.scheme, first, c.dp_flag != 0, 0, h->stream));
+  if (c.scheme == NS_AB2_CN) {
+    int s = enqueue_adi(h);
+    if (s) return s;
+  } else {
+    NS_CUDA(h, launch_vel_bc(h->L, h->us, h->vs, h->ws, h->faces[0], c.bc, h->stream));
+  }
+  int s = enqueue_poisson(h);
+  if (s) return s;
+  CorrectArgs ca{};
+  ca.L = h->L;
+  ca.us = h->us; ca.vs = h->vs; ca.ws = h->ws; ca.dp = h->dp;
+  ca.u = h->u; ca.v = h->v; ca.w = h->w; ca.p = h->p;
+  ca.gx = -c.dt / h->dx; ca.gy = -c.dt / h->dy; ca.gz = -c.dt / h->dz;
+  ca.dp_flag = c.dp_flag; ca.gauge = c.gauge;
+  for (int q = 0; q < 3; ++q) ca.per[q] = c.bc[q] == 1;
+  ca.one = 1.0; ca.mzero = -0.0;
+  NS_CUDA(h, launch_correct(ca, h->stream));
+  return NS_OK;
+}
+
+int build_plans(ns_handle* h) {
+  const ns_config& c = h->cfg;
+  const int nx = c.nx, ny = c.ny, nz = c.nz, M = nx / 2, nxh = M + 1;
+  // Twiddles W_N^m = exp(-2 pi i m / N), computed in long double.
+  auto twid = [](int N, int count, std::vector<double2>& out) {
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int m = 0; m < count; ++m) {
+      const long double th = 2.0L * pi * (long double)m / (long double)N;
+      out.push_back(make_double2((double)cosl(th), (double)(-sinl(th))));
+    }
+  };
+  std::vector<double2> tw;
+  twid(M, M, tw);
+  const size_t o_xr = tw.size();
+  twid(nx, M / 2 + 1, tw);
+  const size_t o_y = tw.size();
+  twid(ny, ny, tw);
+  const size_t o_z = tw.size();
+  twid(nz, nz, tw);
+  NS_CUDA(h, cudaMalloc(&h->tw, tw.size() * sizeof(double2)));
+  NS_CUDA(h, cudaMemcpyAsync(h->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  // Eigenvalues as big_periodic_3D.f90:242-255, inverted with the pipeline's scale.
+  const double pi = 3.1415926535897932;
+  std::vector<double> ex(nxh), ey(ny), ez(nz);
+  for (int i = 0; i < nxh; ++i) { const double s = std::sin(pi * i / nx) / h->dx; ex[i] = s * s; }
+  for (int i = 0; i < ny; ++i) { const double s = std::sin(pi * i / ny) / h->dy; ey[i] = s * s; }
+  for (int i = 0; i < nz; ++i) { const double s = std::sin(pi * i / nz) / h->dz; ez[i] = s * s; }
+  const double scale = 1.0 / (2.0 * (double)nx * (double)ny * (double)nz);
+  std::vector<double> il((size_t)nxh * ny * nz);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nxh; ++i) {
+        const double lam = -4.0 * ((ex[i] + ey[j]) + ez[k]);
+        il[i + (size_t)nxh * (j + (size_t)ny * k)] = (i == 0 && j == 0 && k == 0) ? 0.0 : scale / lam;
+      }
+  NS_CUDA(h, cudaMalloc(&h->inv_lam, il.size() * sizeof(double)));
+  NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, il.data(), il.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  NS_CUDA(h, cudaMalloc(&h->spec, (size_t)nxh * ny * nz * sizeof(double2)));
+  h->plan.nx = nx; h->plan.ny = ny; h->plan.nz = nz; h->plan.nxh = nxh;
+  h->plan.tw_x = h->tw; h->plan.tw_xr = h->tw + o_xr; h->plan.tw_y = h->tw + o_y; h->plan.tw_z = h->tw + o_z;
+  h->plan.inv_lam = h->inv_lam;
+  return NS_OK;
+}
+
+int build_adi(ns_handle* h) {
+  const ns_config& c = h->cfg;
+  if (c.scheme != NS_AB2_CN) return NS_OK;
+  const int ns_[3] = {c.nx, c.ny, c.nz};
+  const double hs[3] = {h->dx, h->dy, h->dz};
+  HostLineSys hs_sys[3][3];
+  size_t total = 0;
+  for (int ax = 0; ax < 3; ++ax)
+    for (int f = 0; f < 3; ++f) {
+      hs_sys[ax][f] = build_cn_system(ns_[ax], c.bc[ax], hs[ax], c.dt, c.nu, f == ax, c.cn_periodic_closure);
+      total += hs_sys[ax][f].l.size() * 3 + hs_sys[ax][f].z.size();
+    }
+  NS_CUDA(h, cudaMalloc(&h->adi_buf, total * sizeof(double)));
+  std::vector<double> host(total);
+  size_t off = 0;
+  for (int ax = 0; ax < 3; ++ax)
+    for (int f = 0; f < 3; ++f) {
+      const HostLineSys& S = hs_sys[ax][f];
+      LineSys& D = h->sys[ax][f];
+      const size_t m = S.l.size();
+      std::memcpy(&host[off], S.l.data(), m * sizeof(double)); D.l = h->adi_buf + off; off += m;
+      std::memcpy(&host[off], S.dinv.data(), m * sizeof(double)); D.dinv = h->adi_buf + off; off += m;
+      std::memcpy(&host[off], S.cu.data(), m * sizeof(double)); D.cu = h->adi_buf + off; off += m;
+      std::memcpy(&host[off], S.z.data(), S.z.size() * sizeof(double)); D.z = h->adi_buf + off; off += S.z.size();
+      D.s0 = S.s0; D.s1 = S.s1; D.zA = S.zA; D.zB = S.zB; D.lo = S.lo; D.hi = S.hi;
+      D.periodic = S.periodic; D.n = S.n;
+    }
+  NS_CUDA(h, cudaMemcpyAsync(h->adi_buf, host.data(), total * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
+void free_all(ns_handle* h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  double* bufs[] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz, h->us, h->vs, h->ws, h->dp, h->inv_lam, h->adi_buf, h->face_buf};
+  for (double* b : bufs)
+    if (b) cudaFree(b);
+  if (h->spec) cudaFree(h->spec);
+  if (h->tw) cudaFree(h->tw);
+  if (h->diag_bits) cudaFree(h->diag_bits);
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ns_version(void) { return "ns_gpu 0.1 (sm_103a, FP64)"; }
+
+const char* ns_status_string(int s) {
+  switch (s) {
+    case NS_OK: return "ok";
+    case NS_ERR_SHAPE: return "unsupported grid shape";
+    case NS_ERR_CUDA: return "CUDA error";
+    case NS_ERR_NONFINITE: return "non-finite value";
+    case NS_ERR_TIMEOUT: return "device wait timed out";
+    case NS_ERR_UNSUPPORTED_BC: return "unsupported boundary condition";
+    case NS_ERR_ARG: return "bad argument";
+    case NS_ERR_NOMEM: return "out of device memory";
+    default: return "unknown status";
+  }
+}
+
+int ns_config_default(ns_config* c, int nx, int ny, int nz) {
+  if (!c) return NS_ERR_ARG;
+  std::memset(c, 0, sizeof(*c));
+  const double pi = 3.1415926535897932;
+  c->nx = nx; c->ny = ny; c->nz = nz;
+  c->lx = 2.0 * pi; c->ly = 2.0 * pi; c->lz = 2.0 * pi;
+  c->nu = 0.002; c->dt = 2.5e-4;
+  c->scheme = NS_AB2;
+  for (int a = 0; a < 3; ++a) { c->bc[a] = 1; c->pbc[a] = 1; }
+  c->dp_flag = 0; c->gauge = 1; c->mean_dp = 0.0;
+  c->cn_periodic_closure = 0;
+  c->use_graph = 1;
+  return NS_OK;
+}
+
+int ns_create(const ns_config* cfg, ns_handle** out) {
+  if (!cfg || !out) return NS_ERR_ARG;
+  *out = nullptr;
+  std::string msg;
+  int s = validate(*cfg, msg);
+  if (s) {
+    std::fprintf(stderr, "ns_create: %s\n", msg.c_str());
+    return s;
+  }
+  ns_handle* h = new ns_handle();
+  h->cfg = *cfg;
+  h->L = make_layout(cfg->nx, cfg->ny, cfg->nz);
+  h->dx = cfg->lx / cfg->nx; h->dy = cfg->ly / cfg->ny; h->dz = cfg->lz / cfg->nz;
+  auto bail = [&](int code) { free_all(h); delete h; return code; };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(NS_ERR_CUDA);
+  h->own_stream = true;
+  double** fields[] = {&h->u, &h->v, &h->w, &h->p, &h->hx, &h->hy, &h->hz, &h->us, &h->vs, &h->ws, &h->dp};
+  for (double** f : fields) {
+    if (cudaMalloc(f, h->L.fsize * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+    if (cudaMemsetAsync(*f, 0, h->L.fsize * sizeof(double), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+  }
+  const size_t ft = face_total(h->L);
+  if (cudaMalloc(&h->face_buf, ft * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+  if (cudaMemsetAsync(h->face_buf, 0, ft * sizeof(double), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+  for (int set = 0; set < 4; ++set)
+    for (int a = 0; a < 3; ++a)
+      for (int f = 0; f < 4; ++f)
+        for (int d = 0; d < 2; ++d) h->faces[set].ax[a].f[f][d] = h->face_buf + face_offset(h->L, set, a, f, d);
+  if (cudaMalloc(&h->diag_bits, sizeof(unsigned long long)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+  if ((s = build_plans(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
+  if ((s = build_adi(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+  *out = h;
+  return NS_OK;
+}
+
+int ns_destroy(ns_handle* h) {
+  if (!h) return NS_ERR_ARG;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return NS_OK;
+}
+
+const char* ns_last_error(const ns_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int ns_set_stream(ns_handle* h, void* stream) {
+  if (!h) return NS_ERR_ARG;
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  h->stream = (cudaStream_t)stream;
+  h->own_stream = false;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NS_OK;
+}
+
+int ns_synchronize(ns_handle* h) {
+  if (!h) return NS_ERR_ARG;
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
+int ns_set_state(ns_handle* h, const double* u, const double* v, const double* w, const double* p, const double* hx,
+                 const double* hy, const double* hz) {
+  if (!h || !u || !v || !w || !p) return fail(h, NS_ERR_ARG, "u, v, w, p are required");
+  NS_CUDA(h, h2d_field(h, h->u, u, 0));
+  NS_CUDA(h, h2d_field(h, h->v, v, 1));
+  NS_CUDA(h, h2d_field(h, h->w, w, 2));
+  NS_CUDA(h, h2d_field(h, h->p, p, 3));
+  // The extra face slot 0 of a periodic axis mirrors face n.
+  NS_CUDA(h, launch_extra_slots(h->L, h->u, h->v, h->w, h->cfg.bc, h->stream));
+  const bool hist = hx && hy && hz;
+  if (hist) {
+    NS_CUDA(h, h2d_field(h, h->hx, hx, 0));
+    NS_CUDA(h, h2d_field(h, h->hy, hy, 1));
+    NS_CUDA(h, h2d_field(h, h->hz, hz, 2));
+  } else {
+    NS_CUDA(h, cudaMemsetAsync(h->hx, 0, h->L.fsize * sizeof(double), h->stream));
+    NS_CUDA(h, cudaMemsetAsync(h->hy, 0, h->L.fsize * sizeof(double), h->stream));
+    NS_CUDA(h, cudaMemsetAsync(h->hz, 0, h->L.fsize * sizeof(double), h->stream));
+  }
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->first_pending = !hist;
+  h->steps = 0;
+  return NS_OK;
+}
+
+int ns_get_state(ns_handle* h, double* u, double* v, double* w, double* p, double* hx, double* hy, double* hz) {
+  if (!h) return NS_ERR_ARG;
+  if (u) NS_CUDA(h, d2h_field(h, u, h->u, 0));
+  if (v) NS_CUDA(h, d2h_field(h, v, h->v, 1));
+  if (w) NS_CUDA(h, d2h_field(h, w, h->w, 2));
+  if (p) NS_CUDA(h, d2h_field(h, p, h->p, 3));
+  if (hx) NS_CUDA(h, d2h_field(h, hx, h->hx, 0));
+  if (hy) NS_CUDA(h, d2h_field(h, hy, h->hy, 1));
+  if (hz) NS_CUDA(h, d2h_field(h, hz, h->hz, 2));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  // History outside the interior ranges is returned as zero.
+  const ns_config& c = h->cfg;
+  double* hs[3] = {hx, hy, hz};
+  for (int f = 0; f < 3; ++f) {
+    double* a = hs[f];
+    if (!a) continue;
+    const int ex = ext_of(c, f, 0), ey = ext_of(c, f, 1), ez = ext_of(c, f, 2);
+    for (int k = 0; k < ez; ++k)
+      for (int j = 0; j < ey; ++j)
+        for (int i = 0; i < ex; ++i) {
+          const int idx[3] = {i, j, k};
+          bool in = true;
+          for (int ax = 0; ax < 3; ++ax) {
+            const int n = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
+            const int I = idx[ax] + 1;  // Fortran index
+            if (ax == f) in = in && (c.bc[ax] == 1 ? (I >= 1 && I <= n) : (I >= 2 && I <= n));
+            else in = in && (I >= 2 && I <= n + 1);
+          }
+          if (!in) a[i + (size_t)ex * (j + (size_t)ey * k)] = 0.0;
+        }
+  }
+  return NS_OK;
+}
+
+int ns_set_faces(ns_handle* h, int set, const double* const faces[24]) {
+  if (!h || set < 0 || set > 3 || !faces) return fail(h, NS_ERR_ARG, "set must be 0..3");
+  // reference order: field-major (u, v, w, p), then x/y/z, then low/high
+  bool any = false;
+  for (int fld = 0; fld < 4; ++fld)
+    for (int ax = 0; ax < 3; ++ax)
+      for (int side = 0; side < 2; ++side) {
+        const double* src = faces[fld * 6 + ax * 2 + side];
+        const size_t n = plane_size(h->L, ax);
+        std::vector<double> plane(n, 0.0);
+        if (src) {
+          face_to_plane(h->cfg, h->L, ax, fld, src, plane.data());
+          any = true;
+        }
+        double* dst = h->face_buf + face_offset(h->L, set, ax, fld, side);
+        NS_CUDA(h, cudaMemcpyAsync(dst, plane.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        NS_CUDA(h, cudaStreamSynchronize(h->stream));
+      }
+  h->face_set_nonzero[set] = any;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NS_OK;
+}
+
+int ns_step(ns_handle* h, int nsteps) {
+  if (!h || nsteps < 0) return NS_ERR_ARG;
+  for (int it = 0; it < nsteps; ++it) {
+    const bool first = h->first_pending && h->cfg.scheme != NS_EULER;
+    if (first || !h->cfg.use_graph || !h->eager_done) {
+      // Eager launch.  The first steady step also runs eagerly so that every
+      // kernel's attributes are set before the step is captured.
+      int s = enqueue_step(h, first);
+      if (s) return s;
+      if (!first) h->eager_done = true;
+    } else {
+      if (!h->graph) {
+        cudaGraph_t g = nullptr;
+        NS_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int s = enqueue_step(h, false);
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (s) { if (g) cudaGraphDestroy(g); return s; }
+        if (e != cudaSuccess) return fail(h, NS_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+        const cudaError_t e2 = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) return fail(h, NS_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e2));
+      }
+      NS_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+    }
+    h->first_pending = false;
+    h->steps++;
+  }
+  return NS_OK;
+}
+
+int ns_get_diag(ns_handle* h, ns_diag* d) {
+  if (!h || !d) return NS_ERR_ARG;
+  NS_CUDA(h, launch_diag(h->L, h->u, h->v, h->w, 1.0 / h->dx, 1.0 / h->dy, 1.0 / h->dz, h->diag_bits, h->stream));
+  unsigned long long bits = 0;
+  double probe = 0;
+  NS_CUDA(h, cudaMemcpyAsync(&bits, h->diag_bits, sizeof(bits), cudaMemcpyDeviceToHost, h->stream));
+  const ns_config& c = h->cfg;
+  // u(nx/2, ny/2, nz/2) in Fortran indices -> slot (nx/2, ny/2-1, nz/2-1)
+  const long long g = h->L.at(c.nx / 2, c.ny / 2 - 1, c.nz / 2 - 1);
+  NS_CUDA(h, cudaMemcpyAsync(&probe, h->u + g, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  double md;
+  std::memcpy(&md, &bits, sizeof(md));
+  d->max_div = md;
+  d->probe = probe;
+  d->steps_done = h->steps;
+  d->euler_start_pending = h->first_pending ? 1 : 0;
+  d->reserved = 0;
+  if (!std::isfinite(md)) return fail(h, NS_ERR_NONFINITE, "non-finite divergence");
+  return NS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Routine tier
+// ---------------------------------------------------------------------------
+static int routine_conv_diff(ns_handle* h, const double* u, const double* v, const double* w, double* ox, double* oy,
+                             double* oz, int mode) {
+  if (!h || !u || !v || !w || !ox || !oy || !oz) return NS_ERR_ARG;
+  const ns_config& c = h->cfg;
+  // stage the inputs through the state buffers (the session state is saved around the call)
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<double*> save = {h->u, h->v, h->w};
+  double *tu = nullptr, *tv = nullptr, *tw = nullptr;
+  NS_CUDA(h, cudaMalloc(&tu, h->L.fsize * sizeof(double)));
+  NS_CUDA(h, cudaMalloc(&tv, h->L.fsize * sizeof(double)));
+  NS_CUDA(h, cudaMalloc(&tw, h->L.fsize * sizeof(double)));
+  NS_CUDA(h, cudaMemsetAsync(tu, 0, h->L.fsize * sizeof(double), h->stream));
+  NS_CUDA(h, cudaMemsetAsync(tv, 0, h->L.fsize * sizeof(double), h->stream));
+  NS_CUDA(h, cudaMemsetAsync(tw, 0, h->L.fsize * sizeof(double), h->stream));
+  NS_CUDA(h, h2d_field(h, tu, u, 0));
+  NS_CUDA(h, h2d_field(h, tv, v, 1));
+  NS_CUDA(h, h2d_field(h, tw, w, 2));
+  // the extra periodic face slot mirrors face n
+  NS_CUDA(h, launch_extra_slots(h->L, tu, tv, tw, c.bc, h->stream));
+  PredictArgs a = predict_args(h);
+  a.u = tu; a.v = tv; a.w = tw;
+  NS_CUDA(h, launch_predict(a, 0, false, false, mode, h->stream));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  // gather the interior ranges into the reference shapes
+  double* outs[3] = {ox, oy, oz};
+  double* srcs[3] = {h->us, h->vs, h->ws};
+  for (int f = 0; f < 3; ++f) {
+    std::vector<double> full(h->L.fsize);
+    NS_CUDA(h, cudaMemcpyAsync(full.data(), srcs[f], h->L.fsize * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    NS_CUDA(h, cudaStreamSynchronize(h->stream));
+    const int ex = (c.bc[0] == 1 || f != 0) ? c.nx : c.nx - 1;
+    const int ey = (c.bc[1] == 1 || f != 1) ? c.ny : c.ny - 1;
+    const int ez = (c.bc[2] == 1 || f != 2) ? c.nz : c.nz - 1;
+    const int x0 = (f == 0 && c.bc[0] != 1) ? 2 : 1;
+    const int y0 = (f == 1 && c.bc[1] != 1) ? 2 : 1;
+    const int z0 = (f == 2 && c.bc[2] != 1) ? 2 : 1;
+    for (int k = 0; k < ez; ++k)
+      for (int j = 0; j < ey; ++j)
+        for (int i = 0; i < ex; ++i)
+          outs[f][i + (size_t)ex * (j + (size_t)ey * k)] = full[h->L.at(x0 + i, y0 + j, z0 + k)];
+  }
+  cudaFree(tu); cudaFree(tv); cudaFree(tw);
+  (void)save;
+  return NS_OK;
+}
+
+int ns_cal_conv(ns_handle* h, const double* u, const double* v, const double* w, double* cx, double* cy, double* cz) {
+  return routine_conv_diff(h, u, v, w, cx, cy, cz, 1);
+}
+
+int ns_cal_diff(ns_handle* h, const double* u, const double* v, const double* w, double* dx, double* dy, double* dz) {
+  return routine_conv_diff(h, u, v, w, dx, dy, dz, 2);
+}
+
+int ns_poisson(ns_handle* h, const double* rhs, double* dp) {
+  if (!h || !rhs || !dp) return NS_ERR_ARG;
+  const ns_config& c = h->cfg;
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  // Stage rhs into the cell slots of the dp buffer, then transform it.
+  std::vector<double> full((size_t)h->L.fsize, 0.0);
+  for (int k = 0; k < c.nz; ++k)
+    for (int j = 0; j < c.ny; ++j)
+      for (int i = 0; i < c.nx; ++i)
+        full[h->L.at(i + 1, j + 1, k + 1)] = rhs[i + (size_t)c.nx * (j + (size_t)c.ny * k)];
+  NS_CUDA(h, cudaMemcpyAsync(h->us, full.data(), full.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int s = enqueue_poisson(h, h->us);
+  if (s) return s;
+  NS_CUDA(h, d2h_field(h, dp, h->dp, 3));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
+int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star) {
+  if (!h || !u_star || !v_star || !w_star) return NS_ERR_ARG;
+  if (h->cfg.scheme != NS_AB2_CN) return fail(h, NS_ERR_ARG, "ns_adi needs scheme AB2-CN (factors are built for it)");
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  NS_CUDA(h, h2d_field(h, h->us, u_star, 0));
+  NS_CUDA(h, h2d_field(h, h->vs, v_star, 1));
+  NS_CUDA(h, h2d_field(h, h->ws, w_star, 2));
+  int s = enqueue_adi(h);
+  if (s) return s;
+  NS_CUDA(h, d2h_field(h, u_star, h->us, 0));
+  NS_CUDA(h, d2h_field(h, v_star, h->vs, 1));
+  NS_CUDA(h, d2h_field(h, w_star, h->ws, 2));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
+}  // extern "C"

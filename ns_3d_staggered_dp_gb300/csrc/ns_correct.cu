@@ -1,0 +1,99 @@
+// Projection correction (big_periodic_3D.f90:562-567;
+// re_simulation_sub_tstep_interBC_combine.f90:793-802):
+//   dp = dp - dp(1,1,1)   (gauge, periodic driver only)
+//   u = -dt*diff(dp,1,1)/dx + u*,  v = ..., w = ...,  p = dp_flag*p + dp
+// computed over each field's full padded extent, ghosts included, exactly as
+// the reference's whole-array expressions.  The gauge constant cancels in
+// the differences, so it is applied to p only.  The extra face slot 0 of a
+// periodic axis is produced from the same inputs as face n (its periodic
+// image), so both hold the same bits.
+//
+// Also the max|div u| diagnostic (big_periodic_3D.f90:576-579) as an
+// integer atomicMax on the bit patterns of |div| (order-preserving for
+// non-negative doubles; a NaN sorts above every finite value).
+#include "ns_internal.cuh"
+#include "ns_kernels.cuh"
+
+namespace ns {
+
+__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a) {
+  const Layout L = a.L;
+  const int nx2 = L.nx + 2, ny2 = L.ny + 2, nz2 = L.nz + 2;
+  const long long tot = (long long)nx2 * ny2 * nz2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  const int i = (int)(t % nx2);
+  const int j = (int)((t / nx2) % ny2);
+  const int k = (int)(t / ((long long)nx2 * ny2));
+  const FOne c{a.one, a.mzero};
+  const long long g = L.at(i, j, k);
+  const double* __restrict__ dp = a.dp;
+  const double dpc = dp[g];
+  // u: face slots 1..nx+1 along x (slot 0 = image of slot nx when periodic)
+  {
+    int ii = i;
+    if (ii == 0 && a.per[0]) ii = L.nx;
+    if (ii >= 1) {
+      const long long gg = L.at(ii, j, k);
+      a.u[g] = fma(a.gx, fsub(c, dp[gg], dp[gg - 1]), a.us[gg]);
+    }
+  }
+  {
+    int jj = j;
+    if (jj == 0 && a.per[1]) jj = L.ny;
+    if (jj >= 1) {
+      const long long gg = L.at(i, jj, k);
+      a.v[g] = fma(a.gy, fsub(c, dp[gg], dp[gg - L.sy]), a.vs[gg]);
+    }
+  }
+  {
+    int kk = k;
+    if (kk == 0 && a.per[2]) kk = L.nz;
+    if (kk >= 1) {
+      const long long gg = L.at(i, j, kk);
+      a.w[g] = fma(a.gz, fsub(c, dp[gg], dp[gg - L.sz]), a.ws[gg]);
+    }
+  }
+  {
+    double d = dpc;
+    if (a.gauge) d = fsub(c, d, dp[L.at(0, 0, 0)]);
+    a.p[g] = a.dp_flag ? fadd(c, a.p[g], d) : d;
+  }
+}
+
+cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st) {
+  const long long tot = (long long)(a.L.nx + 2) * (a.L.ny + 2) * (a.L.nz + 2);
+  correct_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256) diag_kernel(Layout L, const double* __restrict__ u, const double* __restrict__ v,
+                                                   const double* __restrict__ w, double idx, double idy, double idz,
+                                                   unsigned long long* out) {
+  const long long tot = (long long)L.nx * L.ny * L.nz;
+  unsigned long long best = 0ull;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % L.nx);
+    const int j = 1 + (int)((t / L.nx) % L.ny);
+    const int k = 1 + (int)(t / ((long long)L.nx * L.ny));
+    const long long g = L.at(i, j, k);
+    const double d = (u[g + 1] - u[g]) * idx + (v[g + L.sy] - v[g]) * idy + (w[g + L.sz] - w[g]) * idz;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(d));
+    best = b > best ? b : best;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_down_sync(0xffffffffu, best, o);
+    best = x > best ? x : best;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, best);
+}
+
+cudaError_t launch_diag(const Layout& L, const double* u, const double* v, const double* w, double idx, double idy,
+                        double idz, unsigned long long* out_bits, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out_bits, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  diag_kernel<<<152 * 4, 256, 0, st>>>(L, u, v, w, idx, idy, idz, out_bits);
+  return cudaGetLastError();
+}
+
+}  // namespace ns

@@ -1,0 +1,560 @@
+// Periodic pressure Poisson solve by FFT (big_periodic_3D.f90:215-256 plan and
+// eigenvalues, :498-548 solve): RHS = div(u*)/dt, r2c 3D DFT, divide by
+// lambda = -4 sum sin^2(pi k/n)/h^2 (lambda(0,0,0) = +Inf, so the mean mode is
+// zeroed), c2r with 1/(nx ny nz), dp interior.
+//
+// Five kernels, each streaming lines through shared memory:
+//   x-forward : divergence of u*, v*, w* fused with the r2c transform of each
+//               x-line (an nx/2-point complex FFT of the packed even/odd
+//               samples and the split into nx/2+1 bins)
+//   y-forward : complex FFT along y
+//   z-solve   : complex FFT along z, multiply by 1/(lambda * scale), inverse
+//               FFT along z, all on the line held on chip
+//   y-inverse, x-inverse (c2r, writes dp slots 1..nx)
+// A line of N = R1*R2 points is transformed in two register passes
+// ("four-step"): R1 threads each do an R2-point DFT, a twiddle multiply and a
+// shared-memory transpose, then R1-point DFTs.  Register DFTs are radix-2
+// decimation-in-time with every butterfly in Linzer-Feig FMA form (6 FMAs
+// for a general twiddle, 4 for the trivial ones).  The spectrum is
+// (nx/2+1, ny, nz) complex with x fastest, as the reference's DFTI
+// descriptor (cstrides, :217-221).  The overall scale of the forward split,
+// the inverse split and the 1/N of the backward transform are folded into
+// the inverse-eigenvalue table.
+#include "ns_internal.cuh"
+#include "ns_kernels.cuh"
+
+namespace ns {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Register DFTs
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+__host__ __device__ constexpr int brevc(int i, int bits) {
+  return bits == 0 ? 0 : (((i & 1) << (bits - 1)) | brevc(i >> 1, bits - 1));
+}
+
+// Linzer-Feig constants of W32^q = exp(-2 pi i q / 32), q in [0,16):
+// mode 0: W = f (1 + i t);  mode 1: W = f (t + i).
+__device__ __forceinline__ void lf32(int q, double& f, double& t, int& mode) {
+  switch (q) {
+    case 1: f = 0.9807852804032304; t = -0.19891236737965798; mode = 0; break;
+    case 2: f = 0.9238795325112867; t = -0.4142135623730951; mode = 0; break;
+    case 3: f = 0.8314696123025452; t = -0.6681786379192989; mode = 0; break;
+    case 5: f = -0.8314696123025452; t = -0.668178637919299; mode = 1; break;
+    case 6: f = -0.9238795325112867; t = -0.41421356237309515; mode = 1; break;
+    case 7: f = -0.9807852804032304; t = -0.19891236737965806; mode = 1; break;
+    case 9: f = -0.9807852804032304; t = 0.19891236737965792; mode = 1; break;
+    case 10: f = -0.9238795325112867; t = 0.41421356237309503; mode = 1; break;
+    case 11: f = -0.8314696123025455; t = 0.6681786379192984; mode = 1; break;
+    case 13: f = -0.8314696123025453; t = 0.6681786379192988; mode = 0; break;
+    case 14: f = -0.9238795325112867; t = 0.4142135623730952; mode = 0; break;
+    case 15: f = -0.9807852804032304; t = 0.19891236737965837; mode = 0; break;
+    default: f = 1.0; t = 0.0; mode = 0; break;
+  }
+}
+
+constexpr double SQH = 0.70710678118654752440;  // sqrt(1/2)
+
+// DIT butterfly a' = a + W b, b' = a - W b with W = W32^q (DIR = -1) or its
+// conjugate (DIR = +1).
+template <int DIR>
+__device__ __forceinline__ void bfly(double2& a, double2& b, int q, const FOne& c) {
+  double2 y;
+  double f;
+  if (q == 0) {
+    const double2 a0 = a;
+    a.x = fadd(c, a0.x, b.x); a.y = fadd(c, a0.y, b.y);
+    b.x = fsub(c, a0.x, b.x); b.y = fsub(c, a0.y, b.y);
+    return;
+  }
+  if (q == 8) {  // W = -i (forward) / +i (inverse)
+    const double2 a0 = a, b0 = b;
+    if (DIR < 0) {
+      a.x = fadd(c, a0.x, b0.y); a.y = fsub(c, a0.y, b0.x);
+      b.x = fsub(c, a0.x, b0.y); b.y = fadd(c, a0.y, b0.x);
+    } else {
+      a.x = fsub(c, a0.x, b0.y); a.y = fadd(c, a0.y, b0.x);
+      b.x = fadd(c, a0.x, b0.y); b.y = fsub(c, a0.y, b0.x);
+    }
+    return;
+  }
+  if (q == 4) {  // W = sqrt(1/2)(1 -+ i)
+    if (DIR < 0) { y.x = fadd(c, b.x, b.y); y.y = fsub(c, b.y, b.x); }
+    else { y.x = fsub(c, b.x, b.y); y.y = fadd(c, b.y, b.x); }
+    f = SQH;
+  } else if (q == 12) {  // W = -sqrt(1/2)(1 +- i)
+    if (DIR < 0) { y.x = fsub(c, b.x, b.y); y.y = fadd(c, b.y, b.x); }
+    else { y.x = fadd(c, b.x, b.y); y.y = fsub(c, b.y, b.x); }
+    f = -SQH;
+  } else {
+    double t;
+    int mode;
+    lf32(q, f, t, mode);
+    if (DIR > 0) {  // conjugate root
+      if (mode == 0) t = -t;
+      else { f = -f; t = -t; }
+    }
+    if (mode == 0) { y.x = fma(-t, b.y, b.x); y.y = fma(t, b.x, b.y); }
+    else { y.x = fma(t, b.x, -b.y); y.y = fma(t, b.y, b.x); }
+  }
+  const double2 a0 = a;
+  a.x = fma(f, y.x, a0.x); a.y = fma(f, y.y, a0.y);
+  b.x = fma(-f, y.x, a0.x); b.y = fma(-f, y.y, a0.y);
+}
+
+// In-place R-point DFT (R a power of two, R <= 32), natural order in and out.
+template <int R, int DIR>
+__device__ __forceinline__ void dft(double2 (&x)[R], const FOne& c) {
+  constexpr int B = ilog2c(R);
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int j = brevc(i, B);
+    if (j > i) { const double2 tmp = x[i]; x[i] = x[j]; x[j] = tmp; }
+  }
+#pragma unroll
+  for (int len = 2; len <= R; len <<= 1) {
+#pragma unroll
+    for (int s = 0; s < R; s += len) {
+#pragma unroll
+      for (int k = 0; k < len / 2; ++k) bfly<DIR>(x[s + k], x[s + k + len / 2], k * (32 / len), c);
+    }
+  }
+}
+
+__device__ __forceinline__ double2 cmul(const FOne& c, double2 a, double2 w) {
+  double2 r;
+  r.x = fma(a.x, w.x, -fmul(c, a.y, w.y));
+  r.y = fma(a.x, w.y, fmul(c, a.y, w.x));
+  return r;
+}
+__device__ __forceinline__ double2 cmulc(const FOne& c, double2 a, double2 w) {  // a * conj(w)
+  double2 r;
+  r.x = fma(a.x, w.x, fmul(c, a.y, w.y));
+  r.y = fma(a.y, w.x, -fmul(c, a.x, w.y));
+  return r;
+}
+
+// Four-step split N = R1 * R2 (R1 <= R2), T = R1 threads per line.
+template <int N> struct Split;
+template <> struct Split<8> { static constexpr int R1 = 2, R2 = 4; };
+template <> struct Split<16> { static constexpr int R1 = 4, R2 = 4; };
+template <> struct Split<32> { static constexpr int R1 = 4, R2 = 8; };
+template <> struct Split<64> { static constexpr int R1 = 8, R2 = 8; };
+template <> struct Split<128> { static constexpr int R1 = 8, R2 = 16; };
+template <> struct Split<256> { static constexpr int R1 = 16, R2 = 16; };
+template <> struct Split<512> { static constexpr int R1 = 16, R2 = 32; };
+
+// ---------------------------------------------------------------------------
+// y / z passes: lanes over consecutive kx (coalesced), T threads per line.
+// Shared buffer index for line l: (r * R2 + q) * LPC + l.
+// ---------------------------------------------------------------------------
+constexpr int LPC = 16;
+
+template <int N>
+struct YZ {
+  static constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, T = R1, KQ = R2 / T;
+  __device__ static __forceinline__ int sidx(int r, int q, int l) { return (r * R2 + q) * LPC + l; }
+
+  // Forward step A: thread n1 = t loads x[n1 + R1 n2], R2-point DFT, twiddle, to smem (n1, k2).
+  __device__ static __forceinline__ void fwdA(const double2* __restrict__ g, long long st, double2* sb,
+                                              const double2* __restrict__ tw, int l, int t, const FOne& c) {
+    double2 x[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) x[n2] = g[(long long)(t + R1 * n2) * st];
+    dft<R2, -1>(x, c);
+    sb[sidx(t, 0, l)] = x[0];
+#pragma unroll
+    for (int k2 = 1; k2 < R2; ++k2) sb[sidx(t, k2, l)] = cmul(c, x[k2], __ldg(tw + ((t * k2) % N)));
+  }
+  // Forward step B: for k2 = t + T*q: R1-point DFT over n1 -> X[k2 + R2 k1] in xk[q][k1].
+  __device__ static __forceinline__ void fwdB(double2 (&xk)[KQ][R1], const double2* sb, int l, int t,
+                                              const FOne& c) {
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int k2 = t + T * q;
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) xk[q][n1] = sb[sidx(n1, k2, l)];
+      dft<R1, -1>(xk[q], c);
+    }
+  }
+  // Inverse step A: from X[k2 + R2 k1] held in xk, R1-point inverse DFT, twiddle, to smem (k2, alpha).
+  __device__ static __forceinline__ void invA(double2 (&xk)[KQ][R1], double2* sb, const double2* __restrict__ tw,
+                                              int l, int t, const FOne& c) {
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int k2 = t + T * q;
+      dft<R1, 1>(xk[q], c);
+      sb[sidx(0, k2, l)] = xk[q][0];
+#pragma unroll
+      for (int a = 1; a < R1; ++a) sb[sidx(a, k2, l)] = cmulc(c, xk[q][a], __ldg(tw + ((a * k2) % N)));
+    }
+  }
+  // Inverse step B: thread alpha = t, R2-point inverse DFT over k2, x[alpha + R1 beta] to global.
+  __device__ static __forceinline__ void invB(double2* __restrict__ g, long long st, const double2* sb, int l, int t,
+                                              const FOne& c) {
+    double2 x[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) x[k2] = sb[sidx(t, k2, l)];
+    dft<R2, 1>(x, c);
+#pragma unroll
+    for (int b = 0; b < R2; ++b) g[(long long)(t + R1 * b) * st] = x[b];
+  }
+};
+
+// Line geometry of a y/z-pass block.  Blocks with blockIdx.x < nxh/LPC own
+// LPC consecutive kx at one outer index; the last column of blocks owns the
+// Nyquist plane kx = nx/2, with lanes over LPC consecutive outer indices.
+struct LineGeo {
+  long long base;
+  bool valid;
+};
+__device__ __forceinline__ int yz_nblk(int nxh) { return (nxh - 1 + LPC - 1) / LPC; }
+__device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, int l) {
+  const int M = nxh - 1;
+  const int nblk = yz_nblk(nxh);
+  LineGeo G;
+  int kx, o;
+  if ((int)blockIdx.x < nblk) {
+    kx = blockIdx.x * LPC + l;
+    o = blockIdx.y;
+    G.valid = kx < M;
+    if (!G.valid) kx = 0;
+  } else {
+    kx = M;
+    o = blockIdx.y * LPC + l;
+    G.valid = o < (axis == 1 ? nz : ny);
+    if (!G.valid) o = 0;
+  }
+  if (axis == 1) G.base = kx + (long long)nxh * ny * o;  // line along y at (kx, kz = o)
+  else G.base = kx + (long long)nxh * o;                 // line along z at (kx, ky = o)
+  return G;
+}
+
+template <int N, int DIR>
+__global__ void __launch_bounds__(LPC * Split<N>::R1) fft_y_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+  using F = YZ<N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* sb = reinterpret_cast<double2*>(smem_raw);
+  const int l = threadIdx.x, t = threadIdx.y;
+  const LineGeo G = yz_line(1, P.nxh, P.ny, P.nz, l);
+  if ((int)blockIdx.x == yz_nblk(P.nxh) && blockIdx.y * LPC >= (unsigned)P.nz) return;  // whole block idle
+  double2* g = spec + G.base;
+  const long long st = P.nxh;
+  if (DIR < 0) {
+    if (G.valid) F::fwdA(g, st, sb, P.tw_y, l, t, c);
+    __syncthreads();
+    double2 xk[F::KQ][F::R1];
+    F::fwdB(xk, sb, l, t, c);
+    if (G.valid) {
+#pragma unroll
+      for (int q = 0; q < F::KQ; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < F::R1; ++k1) g[(long long)(t + F::T * q + F::R2 * k1) * st] = xk[q][k1];
+    }
+  } else {
+    double2 xk[F::KQ][F::R1];
+#pragma unroll
+    for (int q = 0; q < F::KQ; ++q)
+#pragma unroll
+      for (int k1 = 0; k1 < F::R1; ++k1)
+        xk[q][k1] = G.valid ? g[(long long)(t + F::T * q + F::R2 * k1) * st] : make_double2(0.0, 0.0);
+    F::invA(xk, sb, P.tw_y, l, t, c);
+    __syncthreads();
+    if (G.valid) F::invB(g, st, sb, l, t, c);
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(LPC * Split<N>::R1) fft_z_solve_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+  using F = YZ<N>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* sb = reinterpret_cast<double2*>(smem_raw);
+  const int l = threadIdx.x, t = threadIdx.y;
+  if ((int)blockIdx.x == yz_nblk(P.nxh) && blockIdx.y * LPC >= (unsigned)P.ny) return;
+  const LineGeo G = yz_line(2, P.nxh, P.ny, P.nz, l);
+  double2* g = spec + G.base;
+  const double* lam = P.inv_lam + G.base;
+  const long long st = (long long)P.nxh * P.ny;
+  if (G.valid) F::fwdA(g, st, sb, P.tw_z, l, t, c);
+  __syncthreads();
+  double2 xk[F::KQ][F::R1];
+  F::fwdB(xk, sb, l, t, c);
+#pragma unroll
+  for (int q = 0; q < F::KQ; ++q)
+#pragma unroll
+    for (int k1 = 0; k1 < F::R1; ++k1) {
+      const double s = G.valid ? __ldg(lam + (long long)(t + F::T * q + F::R2 * k1) * st) : 0.0;
+      xk[q][k1].x = fmul(c, xk[q][k1].x, s);
+      xk[q][k1].y = fmul(c, xk[q][k1].y, s);
+    }
+  __syncthreads();
+  F::invA(xk, sb, P.tw_z, l, t, c);
+  __syncthreads();
+  if (G.valid) F::invB(g, st, sb, l, t, c);
+}
+
+// ---------------------------------------------------------------------------
+// x passes: T threads per line are consecutive lanes (lines are contiguous).
+// Shared buffer per line: R1 rows of (R2 + 1) entries, then the packed
+// M-point spectrum for the real/complex split.
+// ---------------------------------------------------------------------------
+template <int M>
+struct XP {
+  static constexpr int R1 = Split<M>::R1, R2 = Split<M>::R2, T = R1, KQ = R2 / T;
+  static constexpr int LINES = 256 / T;          // lines per CTA
+  static constexpr int ROW = R2 + 1;             // padded row (bank spread)
+  static constexpr int LS = (R1 * ROW > M + 2) ? R1 * ROW : M + 2;  // transpose area, reused by the split
+  __device__ static __forceinline__ int sidx(int r, int q) { return r * ROW + q; }
+};
+
+template <int M, bool FROM_RHS>
+__global__ void __launch_bounds__(256) fft_x_fwd_kernel(FftPlan P, DivArgs d, double2* __restrict__ spec) {
+  using X = XP<M>;
+  constexpr int R1 = X::R1, R2 = X::R2, T = X::T, KQ = X::KQ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const FOne c{d.one, d.mzero};
+  const int t = threadIdx.x, l = threadIdx.y;
+  const int line = blockIdx.x * X::LINES + l;
+  const Layout L = d.L;
+  const int ny = L.ny, nz = L.nz;
+  const bool valid = line < ny * nz;
+  const int j = valid ? 1 + line % ny : 1;
+  const int k = valid ? 1 + line / ny : 1;
+  double2* sb = reinterpret_cast<double2*>(smem_raw) + (long long)l * X::LS;
+  double2* zb = sb;  // the split area reuses the transpose area after a barrier
+  const FOne& cc = c;
+  // Step A: packed input z[m] = r[2m] + i r[2m+1], m = n1 + R1 n2, n1 = t.
+  {
+    double2 x[R2];
+    const double* us = d.us + L.at(0, j, k);
+    const double* vs0 = d.vs + L.at(0, j, k);
+    const double* vs1 = d.vs + L.at(0, j + 1, k);
+    const double* ws0 = d.ws + L.at(0, j, k);
+    const double* ws1 = d.ws + L.at(0, j, k + 1);
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) {
+      const int m = t + R1 * n2;
+      const int s = 2 * m + 1;  // cell slots s, s+1
+      if (FROM_RHS) {  // a given Poisson right-hand side in the cell slots
+        x[n2] = *reinterpret_cast<const double2*>(d.rhs + L.at(s, j, k));
+        continue;
+      }
+      const double2 ua = *reinterpret_cast<const double2*>(us + s);
+      const double ub = us[s + 2];
+      const double2 va = *reinterpret_cast<const double2*>(vs0 + s);
+      const double2 vb = *reinterpret_cast<const double2*>(vs1 + s);
+      const double2 wa = *reinterpret_cast<const double2*>(ws0 + s);
+      const double2 wb = *reinterpret_cast<const double2*>(ws1 + s);
+      double r0 = fmul(cc, fsub(cc, ua.y, ua.x), d.cdx);
+      r0 = fma(fsub(cc, vb.x, va.x), d.cdy, r0);
+      r0 = fma(fsub(cc, wb.x, wa.x), d.cdz, r0);
+      double r1 = fmul(cc, fsub(cc, ub, ua.y), d.cdx);
+      r1 = fma(fsub(cc, vb.y, va.y), d.cdy, r1);
+      r1 = fma(fsub(cc, wb.y, wa.y), d.cdz, r1);
+      x[n2] = make_double2(r0, r1);
+    }
+    dft<R2, -1>(x, cc);
+    sb[X::sidx(t, 0)] = x[0];
+#pragma unroll
+    for (int k2 = 1; k2 < R2; ++k2) sb[X::sidx(t, k2)] = cmul(cc, x[k2], __ldg(P.tw_x + ((t * k2) % M)));
+  }
+  __syncthreads();
+  // Step B: Z[k2 + R2 k1] to the split area.
+  {
+    double2 x[KQ][R1];
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) x[q][n1] = sb[X::sidx(n1, t + T * q)];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int k2 = t + T * q;
+      dft<R1, -1>(x[q], cc);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) zb[k2 + R2 * k1] = x[q][k1];
+    }
+  }
+  __syncthreads();
+  // Split: X[k] = E - F, X[M-k] = conj(E + F), E = Z[k] + conj(Z[M-k]),
+  // F = i W^k (Z[k] - conj(Z[M-k])), W = exp(-2 pi i / nx)   (all times 2).
+  if (valid) {
+    double2* out = spec + (long long)P.nxh * ((j - 1) + (long long)P.ny * (k - 1));
+    for (int kk = t; kk <= M / 2; kk += T) {
+      const double2 zk = zb[kk];
+      const double2 zm = zb[(M - kk) % M];
+      const double2 E = make_double2(fadd(cc, zk.x, zm.x), fsub(cc, zk.y, zm.y));
+      const double2 O = make_double2(fsub(cc, zk.x, zm.x), fadd(cc, zk.y, zm.y));
+      const double2 w = __ldg(P.tw_xr + kk);
+      // F = i * W * O
+      const double2 WO = cmul(cc, O, w);
+      const double2 Fv = make_double2(-WO.y, WO.x);
+      out[kk] = make_double2(fsub(cc, E.x, Fv.x), fsub(cc, E.y, Fv.y));
+      if (kk == 0) out[M] = make_double2(fadd(cc, E.x, Fv.x), 0.0);
+      else if (kk != M / 2) out[M - kk] = make_double2(fadd(cc, E.x, Fv.x), -fadd(cc, E.y, Fv.y));
+    }
+  }
+}
+
+template <int M>
+__global__ void __launch_bounds__(256) fft_x_inv_kernel(FftPlan P, const double2* __restrict__ spec, double* dp,
+                                                        Layout L, FOne c) {
+  using X = XP<M>;
+  constexpr int R1 = X::R1, R2 = X::R2, T = X::T, KQ = X::KQ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int t = threadIdx.x, l = threadIdx.y;
+  const int line = blockIdx.x * X::LINES + l;
+  const int ny = L.ny, nz = L.nz;
+  const bool valid = line < ny * nz;
+  const int j = valid ? 1 + line % ny : 1;
+  const int k = valid ? 1 + line / ny : 1;
+  double2* sb = reinterpret_cast<double2*>(smem_raw) + (long long)l * X::LS;
+  double2* zb = sb;  // the unsplit area is reused by the transpose after a barrier
+  const double2* in = spec + (long long)P.nxh * ((j - 1) + (long long)P.ny * (k - 1));
+  // Unsplit: Z[k] = E + F, Z[M-k] = conj(E - F), E = X[k] + conj(X[M-k]),
+  // F = i conj(W^k) (X[k] - conj(X[M-k]))   (all times 2).
+  if (valid) {
+    for (int kk = t; kk <= M / 2; kk += T) {
+      double2 xk = in[kk];
+      double2 xm = in[M - kk];
+      if (kk == 0) { xk.y = 0.0; xm.y = 0.0; }
+      const double2 E = make_double2(fadd(c, xk.x, xm.x), fsub(c, xk.y, xm.y));
+      const double2 D = make_double2(fsub(c, xk.x, xm.x), fadd(c, xk.y, xm.y));
+      const double2 w = __ldg(P.tw_xr + kk);
+      const double2 WD = cmulc(c, D, w);
+      const double2 Fv = make_double2(-WD.y, WD.x);
+      zb[kk] = make_double2(fadd(c, E.x, Fv.x), fadd(c, E.y, Fv.y));
+      if (kk != 0 && kk != M / 2) zb[M - kk] = make_double2(fsub(c, E.x, Fv.x), -fsub(c, E.y, Fv.y));
+    }
+  }
+  __syncthreads();
+  // Inverse step A: k2 = t + T q, R1-point inverse DFT over k1, twiddle.
+  {
+    double2 x[KQ][R1];
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) x[q][k1] = zb[t + T * q + R2 * k1];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < KQ; ++q) {
+      const int k2 = t + T * q;
+      dft<R1, 1>(x[q], c);
+      sb[X::sidx(0, k2)] = x[q][0];
+#pragma unroll
+      for (int a = 1; a < R1; ++a) sb[X::sidx(a, k2)] = cmulc(c, x[q][a], __ldg(P.tw_x + ((a * k2) % M)));
+    }
+  }
+  __syncthreads();
+  // Inverse step B: alpha = t, R2-point inverse DFT over k2, z[alpha + R1 beta].
+  {
+    double2 x[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) x[k2] = sb[X::sidx(t, k2)];
+    dft<R2, 1>(x, c);
+    if (valid) {
+      double* o = dp + L.at(0, j, k);
+#pragma unroll
+      for (int b = 0; b < R2; ++b) {
+        const int m = t + R1 * b;
+        *reinterpret_cast<double2*>(o + 2 * m + 1) = x[b];
+      }
+    }
+  }
+}
+
+template <int M>
+size_t xp_smem() { return (size_t)XP<M>::LINES * XP<M>::LS * sizeof(double2); }
+template <int N>
+size_t yz_smem() { return (size_t)N * LPC * sizeof(double2); }
+
+template <int M>
+cudaError_t launch_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st) {
+  const size_t sm = xp_smem<M>();
+  auto kern = d.rhs ? fft_x_fwd_kernel<M, true> : fft_x_fwd_kernel<M, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int lines = d.L.ny * d.L.nz;
+  dim3 block(XP<M>::T, XP<M>::LINES);
+  kern<<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, d, spec);
+  return cudaGetLastError();
+}
+template <int M>
+cudaError_t launch_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, FOne c, cudaStream_t st) {
+  const size_t sm = xp_smem<M>();
+  cudaError_t e = cudaFuncSetAttribute(fft_x_inv_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int lines = L.ny * L.nz;
+  dim3 block(XP<M>::T, XP<M>::LINES);
+  fft_x_inv_kernel<M><<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, spec, dp, L, c);
+  return cudaGetLastError();
+}
+template <int N, int DIR>
+cudaError_t launch_y(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
+  const size_t sm = yz_smem<N>();
+  cudaError_t e = cudaFuncSetAttribute(fft_y_kernel<N, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int M = P.nxh - 1;
+  dim3 grid((M + LPC - 1) / LPC + 1, P.nz);
+  dim3 block(LPC, Split<N>::R1);
+  fft_y_kernel<N, DIR><<<grid, block, sm, st>>>(P, spec, c);
+  return cudaGetLastError();
+}
+template <int N>
+cudaError_t launch_z(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
+  const size_t sm = yz_smem<N>();
+  cudaError_t e = cudaFuncSetAttribute(fft_z_solve_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int M = P.nxh - 1;
+  dim3 grid((M + LPC - 1) / LPC + 1, P.ny);
+  dim3 block(LPC, Split<N>::R1);
+  fft_z_solve_kernel<N><<<grid, block, sm, st>>>(P, spec, c);
+  return cudaGetLastError();
+}
+
+#define NS_SIZE_SWITCH(n, CALL) \
+  switch (n) {                  \
+    case 16: CALL(16); break;   \
+    case 32: CALL(32); break;   \
+    case 64: CALL(64); break;   \
+    case 128: CALL(128); break; \
+    case 256: CALL(256); break; \
+    case 512: CALL(512); break; \
+    default: return cudaErrorInvalidValue; \
+  }
+
+}  // namespace
+
+bool fft_size_supported(int nx, int ny, int nz) {
+  auto ok = [](int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512; };
+  return ok(nx) && ok(ny) && ok(nz);
+}
+
+cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* /*rhs_tmp*/, double* dp,
+                               const Layout& L, cudaStream_t st) {
+  const FOne c{d.one, d.mzero};
+  cudaError_t e = cudaSuccess;
+#define X_FWD(n) e = launch_x_fwd<(n) / 2>(P, d, spec, st)
+  NS_SIZE_SWITCH(P.nx, X_FWD)
+#undef X_FWD
+  if (e != cudaSuccess) return e;
+#define Y_FWD(n) e = launch_y<(n), -1>(P, spec, c, st)
+  NS_SIZE_SWITCH(P.ny, Y_FWD)
+#undef Y_FWD
+  if (e != cudaSuccess) return e;
+#define Z_SOL(n) e = launch_z<(n)>(P, spec, c, st)
+  NS_SIZE_SWITCH(P.nz, Z_SOL)
+#undef Z_SOL
+  if (e != cudaSuccess) return e;
+#define Y_INV(n) e = launch_y<(n), 1>(P, spec, c, st)
+  NS_SIZE_SWITCH(P.ny, Y_INV)
+#undef Y_INV
+  if (e != cudaSuccess) return e;
+#define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st)
+  NS_SIZE_SWITCH(P.nx, X_INV)
+#undef X_INV
+  return e;
+}
+
+}  // namespace ns

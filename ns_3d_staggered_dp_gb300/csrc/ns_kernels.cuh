@@ -1,0 +1,163 @@
+// Kernel argument blocks and launchers of the FP64 staggered step.
+#pragma once
+#include "ns_internal.cuh"
+
+namespace ns {
+
+// ---------------------------------------------------------------------------
+// Predictor (ns_predict.cu)
+// ---------------------------------------------------------------------------
+struct PredictArgs {
+  Layout L;
+  const double* u;
+  const double* v;
+  const double* w;
+  const double* p;
+  double* us;
+  double* vs;
+  double* ws;
+  double* hx;  // AB2 history (rhs_?_previous), read and rewritten in place
+  double* hy;
+  double* hz;
+  double one, mzero;
+  int ulo, vlo, wlo;  // first active face along the component's own axis (1 periodic, 2 wall)
+  double cx, cy, cz;  // -1/(4 dx) etc: C = -conv
+  // AB2 / Euler: rhs = k0*u + kx*sWE + ky*sSN + kz*sBT + C
+  double k0, kx, ky, kz;
+  // AB2-CN: u* = c0*u + ca*sWE + cb*sSN + cc*sBT + cC*C + cP*prev
+  double c0, ca, cb, cc, cC, cP;
+  double dt, e1, e2;  // AB2: u* = u + e1*rhs + e2*prev
+  double gpx, gpy, gpz;  // -dt/dx etc. (dp_flag)
+  double ix2, iy2, iz2, lap0;  // diffusion-only mode
+};
+
+// Combine the stencil pieces into u* and rewrite the AB2 history at g.
+template <int SCHEME, bool FIRST>
+__device__ __forceinline__ double predictor_combine(const PredictArgs& a, const FOne& c, double uc, double sWE,
+                                                    double sSN, double sBT, double C, double* __restrict__ hist,
+                                                    long long g) {
+  if (SCHEME == 2) {  // AB2-CN explicit half (big_periodic_3D.f90:398-423)
+    double t = fmul(c, a.c0, uc);
+    t = fma(a.ca, sWE, t);
+    t = fma(a.cb, sSN, t);
+    t = fma(a.cc, sBT, t);
+    t = fma(FIRST ? a.dt : a.cC, C, t);  // Euler start: rhs = nu/2 diff - conv (big_periodic_3D.f90:400-408)
+    if (!FIRST) t = fma(a.cP, hist[g], t);
+    hist[g] = C;  // rhs_?_previous = -conv
+    return t;
+  } else {
+    double rhs = fma(a.k0, uc, C);
+    rhs = fma(a.kz, sBT, rhs);
+    rhs = fma(a.ky, sSN, rhs);
+    rhs = fma(a.kx, sWE, rhs);  // nu*diff - conv
+    double t;
+    if (SCHEME == 1 && !FIRST) {  // AB2 (big_periodic_3D.f90:369-396)
+      t = fma(a.e2, hist[g], uc);
+      t = fma(a.e1, rhs, t);
+    } else {  // Euler, or the Euler start of AB2
+      t = fma(a.dt, rhs, uc);
+    }
+    hist[g] = (SCHEME == 0) ? 0.0 : rhs;
+    return t;
+  }
+}
+
+size_t predict_smem_bytes();
+cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Boundary fills (ns_bc.cu)
+// ---------------------------------------------------------------------------
+// A face plane on the device: full (n2 x n3) plane of the box in internal
+// slot order, for the two axes other than the face's axis.
+struct FacePlanes {
+  // [field 0..3 = u,v,w,p][side 0 = low, 1 = high] for one axis
+  const double* f[4][2];
+};
+struct FaceSet {
+  FacePlanes ax[3];
+};
+
+// vel_bc_staggered (NS_functions.f90:213-310), one axis pass.
+cudaError_t launch_vel_bc(const Layout& L, double* us, double* vs, double* ws, const FaceSet& F, const int bc[3],
+                          cudaStream_t st);
+// Face slot 0 of each periodic axis's face field from face n (after a state load).
+cudaError_t launch_extra_slots(const Layout& L, double* u, double* v, double* w, const int bc[3], cudaStream_t st);
+// pr_bc_staggered (NS_functions.f90:1403-1464), the three axis passes.
+cudaError_t launch_pr_bc(const Layout& L, double* dp, const FaceSet& F, const int pbc[3], double dx, double dy,
+                         double dz, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// ADI (ns_adi.cu)
+// ---------------------------------------------------------------------------
+// Factors of one line system (same for every line of a sweep and field).
+struct LineSys {
+  const double* l;     // forward multipliers, length n_unk
+  const double* dinv;  // 1/pivot
+  const double* cu;    // super-diagonal * dinv
+  const double* z;     // Sherman-Morrison vector (periodic only)
+  double s0, s1;       // correction weights of y[first] and y[last] (periodic only)
+  int zA, zB;          // the correction is applied on [0, zA) and [zB, n_unk)
+  int lo, hi;          // first/last unknown slot along the axis
+  int periodic;        // 1: reduced cyclic system on slots 1..n + copies to slots 0, n+1
+  int n;               // cells along the axis
+};
+struct AdiArgs {
+  Layout L;
+  double* f[3];          // u*, v*, w*
+  LineSys sys[3];        // per field (normal or tangential system)
+  const double* face_lo[3];  // BC row values per field (internal-slot planes), NULL -> 0
+  const double* face_hi[3];
+  int ext_lo[3][2], ext_hi[3][2];  // line-index ranges in the two other axes, per field
+};
+cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Periodic FFT Poisson (ns_fft.cu)
+// ---------------------------------------------------------------------------
+struct FftPlan {
+  int nx, ny, nz, nxh;
+  const double2* tw_x;   // twiddles for the nx/2-point complex FFT (x)
+  const double2* tw_xr;  // r2c split twiddles: exp(-2 pi i k / nx), k < nx/2
+  const double2* tw_y;
+  const double2* tw_z;
+  const double* inv_lam;  // 1/(lambda * nx*ny*nz), (nxh, ny, nz), 0 at the mean mode
+};
+struct DivArgs {
+  Layout L;
+  const double* us;
+  const double* vs;
+  const double* ws;
+  double cdx, cdy, cdz;  // 1/(dx dt) etc.
+  double one, mzero;
+  const double* rhs;     // non-null: transform this right-hand side (cell slots) instead of div(u*)/dt
+};
+cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* rhs_tmp, double* dp,
+                               const Layout& L, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Correction (ns_correct.cu)
+// ---------------------------------------------------------------------------
+struct CorrectArgs {
+  Layout L;
+  const double* us;
+  const double* vs;
+  const double* ws;
+  const double* dp;
+  double* u;
+  double* v;
+  double* w;
+  double* p;
+  double gx, gy, gz;  // -dt/dx etc.
+  int dp_flag;
+  int gauge;
+  int per[3];
+  double one, mzero;
+};
+cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st);
+
+// max|div u| over the interior and probe value (diagnostic).
+cudaError_t launch_diag(const Layout& L, const double* u, const double* v, const double* w, double idx, double idy,
+                        double idz, unsigned long long* out_bits, cudaStream_t st);
+
+}  // namespace ns

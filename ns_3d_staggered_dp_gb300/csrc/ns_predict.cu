@@ -1,0 +1,268 @@
+// Fused predictor: convection (cal_conv, NS_functions.f90:53-158), diffusion
+// (cal_diff, NS_functions.f90:161-210), pressure gradient, Euler/AB2/AB2-CN
+// predictor and AB2 history update (big_periodic_3D.f90:340-423,
+// re_simulation_sub_tstep_interBC_combine.f90:543-654), in one pass over HBM.
+//
+// The divergence-form convection is rebuilt from shared products.  With the
+// factor 1/2 of every two-point mean folded into the constants:
+//   SX[c]  = u[c] + u[c+1]                 (x-mean of u at cell c, times 2)
+//   QXY    = (u[f,J-1] + u[f,J]) * (v[f-1,J] + v[f,J])   at x-face f, y-face J
+//   conv_x = (SX[f]^2 - SX[f-1]^2)/(4dx) + (QXY[J+1]-QXY[J])/(4dy) + (QXZ[K+1]-QXZ[K])/(4dz)
+// which is cal_conv's avg/product/diff sequence with the products shared
+// between conv_x, conv_y and conv_z (uy*vx serves both conv_x and conv_y).
+//
+// Tiling: a CTA owns 32 x-cells by TY y-rows and marches along z through a
+// chunk of KC planes.  Warp w (0..TY) is y-row j0-1+w; warp 0 only computes
+// the products of the low y-halo row.  Products are owned one-sided (cell a
+// owns SX[a], and the face products at faces a+1), so an output cell needs
+// products of its own and its lower neighbours only; lane 0's low x-halo
+// products are computed by a single lane (8 FP64 ops per row and plane).
+// Every FP64 operation is issued in FMA form (see ns_internal.cuh).
+#include "ns_internal.cuh"
+#include "ns_kernels.cuh"
+
+namespace ns {
+
+namespace {
+
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int KC = 32;
+constexpr int SXW = TX + 2;  // smem row width: x in [i0-1, i0+32]
+constexpr int SYH = TY + 2;  // smem rows: y in [j0-1, j0+TY]
+constexpr int PXW = TX + 1;  // product row width: x in [i0-1, i0+31]
+constexpr int PYH = TY + 1;  // product rows: y in [j0-1, j0+TY-1]
+
+struct PredSmem {
+  double u[3][SYH][SXW];
+  double v[3][SYH][SXW];
+  double w[3][SYH][SXW];
+  double p[3][SYH][SXW];
+  double sx2[PYH][PXW];
+  double sy2[PYH][PXW];
+  double sz2[2][PYH][PXW];
+  double qxy[PYH][PXW];
+  double qxz[2][PYH][PXW];
+  double qyz[2][PYH][PXW];
+};
+
+__device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
+
+// Load plane k (clamped into the box) of u, v, w (and p) into ring slot s.
+template <bool DPF>
+__device__ __forceinline__ void load_plane(PredSmem& S, const Layout& L, const double* __restrict__ u,
+                                           const double* __restrict__ v, const double* __restrict__ w,
+                                           const double* __restrict__ p, int i0, int j0, int k, int s, int ps) {
+  const int kk = clampi(k, 0, L.nz + 1);
+  const int nthr = blockDim.x * blockDim.y;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  for (int e = tid; e < SXW * SYH; e += nthr) {
+    const int xx = e % SXW, yy = e / SXW;
+    const int gi = clampi(i0 - 1 + xx, 0, L.nx + 1);
+    const int gj = clampi(j0 - 1 + yy, 0, L.ny + 1);
+    const long long g = L.at(gi, gj, kk);
+    S.u[s][yy][xx] = __ldg(u + g);
+    S.v[s][yy][xx] = __ldg(v + g);
+    S.w[s][yy][xx] = __ldg(w + g);
+    if (DPF) S.p[ps][yy][xx] = __ldg(p + g);
+  }
+}
+
+// Products owned by position (a, b) = smem (x = xa, y = yb) at plane k, using
+// ring slots s0 (plane k) and s1 (plane k+1).  Results go to product index
+// (py, px) = (yb, xa) where xa/yb are smem coordinates of the position.
+__device__ __forceinline__ void products(PredSmem& S, const FOne& c, int xa, int yb, int s0, int s1, int pb) {
+  // SX[a] = u[a] + u[a+1]  (plane k, row b)
+  const double sx = fadd(c, S.u[s0][yb][xa], S.u[s0][yb][xa + 1]);
+  // SY[b] = v[b] + v[b+1]
+  const double sy = fadd(c, S.v[s0][yb][xa], S.v[s0][yb + 1][xa]);
+  // SZ[k] = w[k] + w[k+1]
+  const double sz = fadd(c, S.w[s0][yb][xa], S.w[s1][yb][xa]);
+  // QXY at (x-face a+1, y-face b+1): (u[a+1,b] + u[a+1,b+1]) * (v[a,b+1] + v[a+1,b+1])
+  const double q1 = fmul(c, fadd(c, S.u[s0][yb][xa + 1], S.u[s0][yb + 1][xa + 1]),
+                         fadd(c, S.v[s0][yb + 1][xa], S.v[s0][yb + 1][xa + 1]));
+  // QXZ at (x-face a+1, cell b, z-face k+1): (u[a+1] at k, k+1) * (w[a], w[a+1] at k+1)
+  const double q2 = fmul(c, fadd(c, S.u[s0][yb][xa + 1], S.u[s1][yb][xa + 1]),
+                         fadd(c, S.w[s1][yb][xa], S.w[s1][yb][xa + 1]));
+  // QYZ at (cell a, y-face b+1, z-face k+1): (v[a,b+1] at k, k+1) * (w[a,b], w[a,b+1] at k+1)
+  const double q3 = fmul(c, fadd(c, S.v[s0][yb + 1][xa], S.v[s1][yb + 1][xa]),
+                         fadd(c, S.w[s1][yb][xa], S.w[s1][yb + 1][xa]));
+  S.sx2[yb][xa] = fmul(c, sx, sx);
+  S.sy2[yb][xa] = fmul(c, sy, sy);
+  S.sz2[pb][yb][xa] = fmul(c, sz, sz);
+  S.qxy[yb][xa] = q1;
+  S.qxz[pb][yb][xa] = q2;
+  S.qyz[pb][yb][xa] = q3;
+}
+
+// Products for z-face k only (the warm-up plane): SZ at cell k-1 (planes
+// k-1, k) and QXZ/QYZ at z-face k.  s0 = plane k-1, s1 = plane k.
+__device__ __forceinline__ void products_zface(PredSmem& S, const FOne& c, int xa, int yb, int s0, int s1, int pb) {
+  const double sz = fadd(c, S.w[s0][yb][xa], S.w[s1][yb][xa]);
+  const double q2 = fmul(c, fadd(c, S.u[s0][yb][xa + 1], S.u[s1][yb][xa + 1]),
+                         fadd(c, S.w[s1][yb][xa], S.w[s1][yb][xa + 1]));
+  const double q3 = fmul(c, fadd(c, S.v[s0][yb + 1][xa], S.v[s1][yb + 1][xa]),
+                         fadd(c, S.w[s1][yb][xa], S.w[s1][yb + 1][xa]));
+  S.sz2[pb][yb][xa] = fmul(c, sz, sz);
+  S.qxz[pb][yb][xa] = q2;
+  S.qyz[pb][yb][xa] = q3;
+}
+
+}  // namespace
+
+// MODE: 0 predictor, 1 conv only (writes conv into us/vs/ws), 2 diffusion only.
+template <int SCHEME, bool FIRST, bool DPF, int MODE>
+__global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PredSmem& S = *reinterpret_cast<PredSmem*>(smem_raw);
+  const Layout L = a.L;
+  const FOne c{a.one, a.mzero};
+  const int lane = threadIdx.x;
+  const int wy = threadIdx.y;  // 0..TY
+  const int i0 = 1 + TX * blockIdx.x;
+  const int j0 = 1 + TY * blockIdx.y;
+  const int k0 = 1 + KC * blockIdx.z;
+  const int k1 = min(k0 + KC, L.nz + 1);
+  // smem coordinates of this thread's position: x = i0-1+lane+1 -> xa = lane+1; y = j0-1+wy -> yb = wy
+  const int xa = lane + 1;
+  const int yb = wy;
+
+  // Warm-up: planes k0-1 and k0 in ring slots, products at z-face k0.
+  load_plane<DPF>(S, L, a.u, a.v, a.w, a.p, i0, j0, k0 - 1, (k0 - 1) % 3, (k0 - 1) % 3);
+  load_plane<DPF>(S, L, a.u, a.v, a.w, a.p, i0, j0, k0, k0 % 3, k0 % 3);
+  __syncthreads();
+  if (MODE != 2) {
+    products_zface(S, c, xa, yb, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
+    if (lane == 0) products_zface(S, c, 0, yb, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
+  }
+
+  const int i = i0 + lane;
+  const int j = j0 - 1 + wy;
+  const int nx = L.nx, ny = L.ny, nz = L.nz;
+  const bool in_xy = (wy >= 1) && (i <= nx) && (j <= ny);
+  const bool act_u = in_xy && (i >= a.ulo);
+  const bool act_v = in_xy && (j >= a.vlo);
+
+  for (int k = k0; k < k1; ++k) {
+    const int s0 = k % 3, s1 = (k + 1) % 3, sm = (k + 2) % 3;  // planes k, k+1, k-1
+    const int pb = k & 1, pbm = (k - 1) & 1;
+    load_plane<DPF>(S, L, a.u, a.v, a.w, a.p, i0, j0, k + 1, s1, s1);
+    __syncthreads();
+    if (MODE != 2) {
+      products(S, c, xa, yb, s0, s1, pb);
+      if (lane == 0) products(S, c, 0, yb, s0, s1, pb);
+    }
+    __syncthreads();
+    const bool act_w = (k >= a.wlo);
+    if (in_xy) {
+      const long long g = L.at(i, j, k);
+      // ---- x-component at x-face i ----
+      if (act_u) {
+        const double uc = S.u[s0][yb][xa];
+        const double sWE = fadd(c, S.u[s0][yb][xa - 1], S.u[s0][yb][xa + 1]);
+        const double sSN = fadd(c, S.u[s0][yb - 1][xa], S.u[s0][yb + 1][xa]);
+        const double sBT = fadd(c, S.u[sm][yb][xa], S.u[s1][yb][xa]);
+        double C = 0.0;
+        if (MODE != 2) {
+          const double dX = fsub(c, S.sx2[yb][xa], S.sx2[yb][xa - 1]);
+          const double dY = fsub(c, S.qxy[yb][xa - 1], S.qxy[yb - 1][xa - 1]);
+          const double dZ = fsub(c, S.qxz[pb][yb][xa - 1], S.qxz[pbm][yb][xa - 1]);
+          C = fmul(c, dX, a.cx);
+          C = fma(dY, a.cy, C);
+          C = fma(dZ, a.cz, C);  // C = -conv_x
+        }
+        double out;
+        if (MODE == 1) {
+          out = -C;
+        } else if (MODE == 2) {
+          out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, uc))));
+        } else {
+          out = predictor_combine<SCHEME, FIRST>(a, c, uc, sWE, sSN, sBT, C, a.hx, g);
+          if (DPF) out = fma(a.gpx, fsub(c, S.p[s0][yb][xa], S.p[s0][yb][xa - 1]), out);
+        }
+        a.us[g] = out;
+      }
+      // ---- y-component at y-face j ----
+      if (act_v) {
+        const double vc = S.v[s0][yb][xa];
+        const double sWE = fadd(c, S.v[s0][yb][xa - 1], S.v[s0][yb][xa + 1]);
+        const double sSN = fadd(c, S.v[s0][yb - 1][xa], S.v[s0][yb + 1][xa]);
+        const double sBT = fadd(c, S.v[sm][yb][xa], S.v[s1][yb][xa]);
+        double C = 0.0;
+        if (MODE != 2) {
+          const double dX = fsub(c, S.qxy[yb - 1][xa], S.qxy[yb - 1][xa - 1]);
+          const double dY = fsub(c, S.sy2[yb][xa], S.sy2[yb - 1][xa]);
+          const double dZ = fsub(c, S.qyz[pb][yb - 1][xa], S.qyz[pbm][yb - 1][xa]);
+          C = fmul(c, dX, a.cx);
+          C = fma(dY, a.cy, C);
+          C = fma(dZ, a.cz, C);
+        }
+        double out;
+        if (MODE == 1) {
+          out = -C;
+        } else if (MODE == 2) {
+          out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, vc))));
+        } else {
+          out = predictor_combine<SCHEME, FIRST>(a, c, vc, sWE, sSN, sBT, C, a.hy, g);
+          if (DPF) out = fma(a.gpy, fsub(c, S.p[s0][yb][xa], S.p[s0][yb - 1][xa]), out);
+        }
+        a.vs[g] = out;
+      }
+      // ---- z-component at z-face k ----
+      if (act_w) {
+        const double wc = S.w[s0][yb][xa];
+        const double sWE = fadd(c, S.w[s0][yb][xa - 1], S.w[s0][yb][xa + 1]);
+        const double sSN = fadd(c, S.w[s0][yb - 1][xa], S.w[s0][yb + 1][xa]);
+        const double sBT = fadd(c, S.w[sm][yb][xa], S.w[s1][yb][xa]);
+        double C = 0.0;
+        if (MODE != 2) {
+          const double dX = fsub(c, S.qxz[pbm][yb][xa], S.qxz[pbm][yb][xa - 1]);
+          const double dY = fsub(c, S.qyz[pbm][yb][xa], S.qyz[pbm][yb - 1][xa]);
+          const double dZ = fsub(c, S.sz2[pb][yb][xa], S.sz2[pbm][yb][xa]);
+          C = fmul(c, dX, a.cx);
+          C = fma(dY, a.cy, C);
+          C = fma(dZ, a.cz, C);
+        }
+        double out;
+        if (MODE == 1) {
+          out = -C;
+        } else if (MODE == 2) {
+          out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, wc))));
+        } else {
+          out = predictor_combine<SCHEME, FIRST>(a, c, wc, sWE, sSN, sBT, C, a.hz, g);
+          if (DPF) out = fma(a.gpz, fsub(c, S.p[s0][yb][xa], S.p[sm][yb][xa]), out);
+        }
+        a.ws[g] = out;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+size_t predict_smem_bytes() { return sizeof(PredSmem); }
+
+template <int SCHEME, bool FIRST, bool DPF, int MODE>
+static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st) {
+  auto kern = predict_kernel<SCHEME, FIRST, DPF, MODE>;
+  const size_t sm = sizeof(PredSmem);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  dim3 grid((a.L.nx + TX - 1) / TX, (a.L.ny + TY - 1) / TY, (a.L.nz + KC - 1) / KC);
+  dim3 block(TX, TY + 1);
+  kern<<<grid, block, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st) {
+  if (mode == 1) return launch_t<0, false, false, 1>(a, st);
+  if (mode == 2) return launch_t<0, false, false, 2>(a, st);
+#define NS_PRED_CASE(S, F, D) \
+  if (scheme == S && first == F && dpf == D) return launch_t<S, F, D, 0>(a, st);
+  NS_PRED_CASE(0, false, false) NS_PRED_CASE(0, false, true) NS_PRED_CASE(0, true, false) NS_PRED_CASE(0, true, true)
+  NS_PRED_CASE(1, false, false) NS_PRED_CASE(1, false, true) NS_PRED_CASE(1, true, false) NS_PRED_CASE(1, true, true)
+  NS_PRED_CASE(2, false, false) NS_PRED_CASE(2, false, true) NS_PRED_CASE(2, true, false) NS_PRED_CASE(2, true, true)
+#undef NS_PRED_CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ns

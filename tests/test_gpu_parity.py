@@ -1,0 +1,157 @@
+"""CUDA path vs the CPU oracle, through the C ABI (libns_gpu.so).
+
+Tolerances: the step is FP64 with the same algebra as the reference but
+different rounding (FMA folding, MKL vs our FFT/Thomas); routine-level
+results must agree to a relative L2 of 1e-12, ten full steps to 1e-10 per
+field (the benchmark spec's bound), and max|div u| <= 1e-12 after every step.
+"""
+import numpy as np
+import pytest
+
+from oracle import ns_oracle as O
+from tests.helpers import random_state, rel_l2, tgv_state
+
+pytestmark = pytest.mark.gpu
+
+ROUTINE_TOL = 1e-12
+STEP_TOL = 1e-10
+DIV_TOL = 1e-12
+
+
+def to_ns(cfg, **kw):
+    from ns_3d_staggered_dp_gb300 import make_config
+    return make_config(cfg.nx, cfg.ny, cfg.nz, lx=cfg.lx, ly=cfg.ly, lz=cfg.lz, nu=cfg.nu, dt=cfg.dt,
+                       scheme=cfg.scheme, bc=cfg.bc, pbc=cfg.pbc, dp_flag=cfg.dp_flag, gauge=cfg.gauge,
+                       mean_dp=cfg.mean_dp, **kw)
+
+
+def session(cfg, **kw):
+    from ns_3d_staggered_dp_gb300 import Session
+    return Session(to_ns(cfg, **kw))
+
+
+GRIDS = [(32, 32, 32, 1.0, 1.0, 1.0), (32, 16, 64, 1.0, 0.5, 1.7)]
+
+
+@pytest.mark.parametrize("g", GRIDS)
+def test_cal_conv_diff(g):
+    nx, ny, nz, fx, fy, fz = g
+    cfg = O.Config(nx, ny, nz, lx=2 * np.pi * fx, ly=2 * np.pi * fy, lz=2 * np.pi * fz)
+    st = random_state(cfg, 11)
+    dx, dy, dz = cfg.h
+    ref_c = O.cal_conv(st.u, st.v, st.w, *cfg.bc, dx, dy, dz)
+    ref_d = O.cal_diff(st.u, st.v, st.w, *cfg.bc, dx * dx, dy * dy, dz * dz)
+    with session(cfg) as s:
+        got_c = s.cal_conv(st.u, st.v, st.w)
+        got_d = s.cal_diff(st.u, st.v, st.w)
+    for a, b in zip(got_c, ref_c):
+        assert a.shape == b.shape
+        assert rel_l2(a, b) < ROUTINE_TOL
+    for a, b in zip(got_d, ref_d):
+        assert rel_l2(a, b) < ROUTINE_TOL
+
+
+@pytest.mark.parametrize("g", GRIDS + [(16, 16, 16, 1.0, 1.0, 1.0), (64, 32, 16, 1.0, 1.0, 1.0)])
+def test_fft_poisson(g):
+    nx, ny, nz, fx, fy, fz = g
+    cfg = O.Config(nx, ny, nz, lx=2 * np.pi * fx, ly=2 * np.pi * fy, lz=2 * np.pi * fz)
+    rng = np.random.default_rng(5)
+    R = rng.standard_normal((nx, ny, nz))
+    R -= R.mean()
+    dx, dy, dz = cfg.h
+    ref = np.zeros((nx + 2, ny + 2, nz + 2))
+    ref[1:-1, 1:-1, 1:-1] = O.fft_poisson(R, O.fft_eigenvalues(nx, ny, nz, dx, dy, dz))
+    O.pr_bc_staggered(ref, O.Faces.zeros(nx, ny, nz), cfg.pbc, dx, dy, dz)
+    with session(cfg) as s:
+        got = s.poisson(R)
+    assert rel_l2(got, ref) < ROUTINE_TOL
+    # operator check: the interior solves the restated Poisson operator
+    L = O.poisson_lhs_staggered(nx, ny, nz, dx * dx, dy * dy, dz * dz, (1, 1, 1))
+    res = L @ got[1:-1, 1:-1, 1:-1].reshape(-1, order="F") - R.reshape(-1, order="F")
+    assert np.abs(res).max() < 1e-9 * np.abs(R).max() * max(1.0, 1 / dx ** 2)
+
+
+@pytest.mark.parametrize("closure", [0, 1])
+@pytest.mark.parametrize("g", GRIDS)
+def test_adi_periodic(g, closure):
+    nx, ny, nz, fx, fy, fz = g
+    cfg = O.Config(nx, ny, nz, lx=2 * np.pi * fx, ly=2 * np.pi * fy, lz=2 * np.pi * fz, nu=0.05, dt=0.01,
+                   scheme=O.AB2_CN)
+    st = random_state(cfg, 3)
+    dx, dy, dz = cfg.h
+    orig = O.mat_cn
+    if closure:
+        def fixed(n, bc, dx2, dt0, nu):
+            A, B = orig(n, bc, dx2, dt0, nu)
+            if bc == 1:
+                of = A[1, 0]; A[0, n] = 0.0; A[0, n - 1] = of
+            return A, B
+        O.mat_cn = fixed
+    try:
+        cnf = O.CNFactors(nx, ny, nz, cfg.bc, dx * dx, dy * dy, dz * dz, cfg.dt, cfg.nu)
+        ref = O.adi_sweeps(st.u, st.v, st.w, cnf, cfg.bc)
+    finally:
+        O.mat_cn = orig
+    with session(cfg, cn_periodic_closure=closure) as s:
+        got = s.adi(st.u, st.v, st.w)
+    for a, b in zip(got, ref):
+        assert rel_l2(a, b) < ROUTINE_TOL
+
+
+def _run_compare(cfg, st, nsteps, **kw):
+    ref = st.copy()
+    with session(cfg, **kw) as s:
+        s.set_state(st.u, st.v, st.w, st.p, None if st.first else (st.px, st.py, st.pz))
+        for _ in range(nsteps):
+            ref = O.step(ref, cfg)
+            s.step(1)
+            d = s.diag()
+            assert d["max_div"] < DIV_TOL * max(1.0, np.abs(ref.u).max() / min(cfg.h))
+        got = s.get_state()
+    for k, r in (("u", ref.u), ("v", ref.v), ("w", ref.w), ("p", ref.p), ("hx", ref.px), ("hy", ref.py),
+                 ("hz", ref.pz)):
+        err = rel_l2(got[k], r)
+        assert err < STEP_TOL, (k, err)
+    return got, ref
+
+
+@pytest.mark.parametrize("scheme", [O.EULER, O.AB2, O.AB2_CN])
+@pytest.mark.parametrize("dp_flag", [0, 1])
+def test_step_tgv_32(scheme, dp_flag):
+    """32^3 Taylor-Green + noise, nu = 0.01, dt = 0.01, 10 steps from the Euler start."""
+    cfg = O.Config(32, 32, 32, nu=0.01, dt=0.01, scheme=scheme, dp_flag=dp_flag)
+    st = tgv_state(cfg)
+    _run_compare(cfg, st, 10)
+
+
+def test_step_restart_with_history():
+    """Restart (history given): no Euler start, AB2-CN on a non-cubic box."""
+    cfg = O.Config(32, 16, 64, lx=2 * np.pi, ly=np.pi, lz=4.0, nu=0.02, dt=0.005, scheme=O.AB2_CN)
+    st = random_state(cfg, 21, amp=0.1, history=True)
+    _run_compare(cfg, st, 5)
+
+
+def test_step_graph_matches_eager():
+    """Graph replay gives bitwise the same state as eager launches."""
+    cfg = O.Config(32, 32, 32, nu=0.01, dt=0.01, scheme=O.AB2_CN)
+    st = tgv_state(cfg)
+    outs = []
+    for g in (0, 1):
+        with session(cfg, use_graph=g) as s:
+            s.set_state(st.u, st.v, st.w, st.p)
+            s.step(6)
+            outs.append(s.get_state())
+    for k in ("u", "v", "w", "p", "hx"):
+        assert np.array_equal(outs[0][k], outs[1][k])
+
+
+def test_determinism():
+    cfg = O.Config(32, 32, 32, nu=0.01, dt=0.01, scheme=O.AB2)
+    st = tgv_state(cfg)
+    outs = []
+    for _ in range(2):
+        with session(cfg) as s:
+            s.set_state(st.u, st.v, st.w, st.p)
+            s.step(4)
+            outs.append(s.get_state())
+    assert all(np.array_equal(outs[0][k], outs[1][k]) for k in ("u", "v", "w", "p"))
