@@ -156,6 +156,22 @@ int ns_poisson(ns_handle* h, const double* rhs, double* dp);
  * (big_periodic_3D.f90:425-489; re_simulation_sub_tstep_interBC_combine.f90:656-701). */
 int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star);
 
+/* ------------------------------------------------------------------------
+ * Tracing (the per-phase SYSTEM_CLOCK prints of big_periodic_3D.f90:328-569).
+ * ------------------------------------------------------------------------ */
+typedef struct ns_kernel_time {
+  char name[32];        /* kernel (phase) name: predict, adi_x, fft_z_solve, ... */
+  double ms;            /* summed device time between CUDA events              */
+  long long launches;   /* marks recorded under this name                      */
+} ns_kernel_time;
+
+/* Run nsteps steps with a CUDA event after every kernel and return the
+ * per-kernel device time (eager launches, not the captured graph). */
+int ns_profile(ns_handle* h, int nsteps, ns_kernel_time* out, int max_out, int* n_out);
+
+/* Number of kernels this handle has launched (graph replays included). */
+int ns_launch_count(const ns_handle* h, long long* launches);
+
 /* Version string of the library build. */
 const char* ns_version(void);
 

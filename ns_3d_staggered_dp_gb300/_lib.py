@@ -31,6 +31,10 @@ class NSConfig(C.Structure):
     ]
 
 
+class NSKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("ms", C.c_double), ("launches", C.c_longlong)]
+
+
 class NSDiag(C.Structure):
     _fields_ = [("max_div", C.c_double), ("probe", C.c_double), ("steps_done", C.c_longlong),
                 ("euler_start_pending", C.c_int), ("reserved", C.c_int)]
@@ -55,6 +59,8 @@ SIGNATURES = {
     "ns_cal_diff": (C.c_int, [C.c_void_p] + [_DP] * 6),
     "ns_poisson": (C.c_int, [C.c_void_p, _DP, _DP]),
     "ns_adi": (C.c_int, [C.c_void_p, _DP, _DP, _DP]),
+    "ns_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(NSKernelTime), C.c_int, C.POINTER(C.c_int)]),
+    "ns_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "ns_version": (C.c_char_p, []),
 }
 

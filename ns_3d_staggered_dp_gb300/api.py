@@ -147,6 +147,18 @@ class Session:
         return {"max_div": d.max_div, "probe": d.probe, "steps": d.steps_done,
                 "euler_start_pending": bool(d.euler_start_pending)}
 
+    def profile(self, nsteps=1):
+        """Per-kernel device time (ms) over nsteps eager steps: {name: (ms, launches)}."""
+        arr = (_lib.NSKernelTime * 64)()
+        n = C.c_int()
+        self._check(self.lib.ns_profile(self.h, nsteps, arr, 64, C.byref(n)))
+        return {arr[i].name.decode(): (arr[i].ms, arr[i].launches) for i in range(n.value)}
+
+    def launch_count(self):
+        v = C.c_longlong()
+        self._check(self.lib.ns_launch_count(self.h, C.byref(v)))
+        return v.value
+
     # routine tier -----------------------------------------------------------
     def _conv_shapes(self):
         c = self.cfg

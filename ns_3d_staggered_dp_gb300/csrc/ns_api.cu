@@ -126,6 +126,7 @@ struct ns_handle {
   ns_config cfg;
   Layout L;
   cudaStream_t stream = nullptr;
+  cudaStream_t cap_stream = nullptr;  // private stream for graph capture
   bool own_stream = false;
   double dx, dy, dz;
   // device fields
@@ -151,6 +152,11 @@ struct ns_handle {
   // graphs
   cudaGraphExec_t graph = nullptr;
   bool eager_done = false;
+  long long graph_launches = 0;
+  // launch counting and per-kernel timing (ns_profile)
+  long long launches = 0;
+  bool profiling = false;
+  std::vector<std::pair<std::string, cudaEvent_t>> prof_events;
 };
 
 namespace {
@@ -257,6 +263,25 @@ int validate(const ns_config& c, std::string& msg) {
   return NS_OK;
 }
 
+// After every kernel launch: count it and, while profiling, record an event.
+void mark(ns_handle* h, const char* name, int nkernels = 1) {
+  h->launches += nkernels;
+  if (h->profiling) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) == cudaSuccess) {
+      cudaEventRecord(e, h->stream);
+      h->prof_events.emplace_back(name, e);
+    }
+  }
+}
+void mark_cb(void* ctx, const char* name) { mark(static_cast<ns_handle*>(ctx), name); }
+Marker marker(ns_handle* h) {
+  Marker m;
+  m.fn = mark_cb;
+  m.ctx = h;
+  return m;
+}
+
 PredictArgs predict_args(ns_handle* h) {
   const ns_config& c = h->cfg;
   PredictArgs a{};
@@ -299,6 +324,7 @@ int enqueue_adi(ns_handle* h) {
     }
     (void)c;
     NS_CUDA(h, launch_adi(ax, a, h->stream));
+    mark(h, ax == 0 ? "adi_x" : (ax == 1 ? "adi_y" : "adi_z"));
   }
   return NS_OK;
 }
@@ -311,8 +337,9 @@ int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
   d.us = h->us; d.vs = h->vs; d.ws = h->ws;
   d.cdx = 1.0 / (h->dx * c.dt); d.cdy = 1.0 / (h->dy * c.dt); d.cdz = 1.0 / (h->dz * c.dt);
   d.one = 1.0; d.mzero = -0.0;
-  NS_CUDA(h, launch_fft_poisson(h->plan, d, h->spec, nullptr, h->dp, h->L, h->stream));
+  NS_CUDA(h, launch_fft_poisson(h->plan, d, h->spec, h->dp, h->L, h->stream, marker(h)));
   NS_CUDA(h, launch_pr_bc(h->L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, h->dz, h->stream));
+  mark(h, "pr_bc", 3);
   return NS_OK;
 }
 
@@ -320,11 +347,13 @@ int enqueue_step(ns_handle* h, bool first) {
   const ns_config& c = h->cfg;
   PredictArgs a = predict_args(h);
   NS_CUDA(h, launch_predict(a, c.scheme, first, c.dp_flag != 0, 0, h->stream));
+  mark(h, "predict");
   if (c.scheme == NS_AB2_CN) {
     int s = enqueue_adi(h);
     if (s) return s;
   } else {
     NS_CUDA(h, launch_vel_bc(h->L, h->us, h->vs, h->ws, h->faces[0], c.bc, h->stream));
+    mark(h, "vel_bc", 3);
   }
   int s = enqueue_poisson(h);
   if (s) return s;
@@ -337,6 +366,7 @@ int enqueue_step(ns_handle* h, bool first) {
   for (int q = 0; q < 3; ++q) ca.per[q] = c.bc[q] == 1;
   ca.one = 1.0; ca.mzero = -0.0;
   NS_CUDA(h, launch_correct(ca, h->stream));
+  mark(h, "correct");
   return NS_OK;
 }
 
@@ -426,6 +456,7 @@ void free_all(ns_handle* h) {
   if (h->tw) cudaFree(h->tw);
   if (h->diag_bits) cudaFree(h->diag_bits);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
 }
 
 }  // namespace
@@ -479,6 +510,7 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
   auto bail = [&](int code) { free_all(h); delete h; return code; };
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(NS_ERR_CUDA);
   h->own_stream = true;
+  if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(NS_ERR_CUDA);
   double** fields[] = {&h->u, &h->v, &h->w, &h->p, &h->hx, &h->hy, &h->hz, &h->us, &h->vs, &h->ws, &h->dp};
   for (double** f : fields) {
     if (cudaMalloc(f, h->L.fsize * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
@@ -567,19 +599,23 @@ int ns_get_state(ns_handle* h, double* u, double* v, double* w, double* p, doubl
     double* a = hs[f];
     if (!a) continue;
     const int ex = ext_of(c, f, 0), ey = ext_of(c, f, 1), ez = ext_of(c, f, 2);
+    // interior range (0-based) per axis: the field's own axis 1..n-1 or 0..n-1, others 1..n
+    int lo[3], hi[3];
+    for (int ax = 0; ax < 3; ++ax) {
+      const int n = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
+      if (ax == f) { lo[ax] = c.bc[ax] == 1 ? 0 : 1; hi[ax] = n - 1; }
+      else { lo[ax] = 1; hi[ax] = n; }
+    }
     for (int k = 0; k < ez; ++k)
-      for (int j = 0; j < ey; ++j)
-        for (int i = 0; i < ex; ++i) {
-          const int idx[3] = {i, j, k};
-          bool in = true;
-          for (int ax = 0; ax < 3; ++ax) {
-            const int n = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
-            const int I = idx[ax] + 1;  // Fortran index
-            if (ax == f) in = in && (c.bc[ax] == 1 ? (I >= 1 && I <= n) : (I >= 2 && I <= n));
-            else in = in && (I >= 2 && I <= n + 1);
-          }
-          if (!in) a[i + (size_t)ex * (j + (size_t)ey * k)] = 0.0;
+      for (int j = 0; j < ey; ++j) {
+        double* row = a + (size_t)ex * (j + (size_t)ey * k);
+        if (k < lo[2] || k > hi[2] || j < lo[1] || j > hi[1]) {
+          std::memset(row, 0, sizeof(double) * ex);
+          continue;
         }
+        for (int i = 0; i < lo[0]; ++i) row[i] = 0.0;
+        for (int i = hi[0] + 1; i < ex; ++i) row[i] = 0.0;
+      }
   }
   return NS_OK;
 }
@@ -619,10 +655,21 @@ int ns_step(ns_handle* h, int nsteps) {
       if (!first) h->eager_done = true;
     } else {
       if (!h->graph) {
+        // Capture on the handle's private stream (the caller's stream may be
+        // the legacy default stream, which cannot be captured); the graph is
+        // then replayed on the caller's stream.
         cudaGraph_t g = nullptr;
-        NS_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        NS_CUDA(h, cudaStreamSynchronize(h->stream));
+        cudaStream_t user = h->stream;
+        h->stream = h->cap_stream;
+        cudaError_t eb = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (eb != cudaSuccess) { h->stream = user; return fail(h, NS_ERR_CUDA, cudaGetErrorString(eb)); }
+        const long long before = h->launches;
         const int s = enqueue_step(h, false);
+        h->graph_launches = h->launches - before;
+        h->launches = before;
         const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        h->stream = user;
         if (s) { if (g) cudaGraphDestroy(g); return s; }
         if (e != cudaSuccess) return fail(h, NS_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
         const cudaError_t e2 = cudaGraphInstantiate(&h->graph, g, 0);
@@ -630,10 +677,61 @@ int ns_step(ns_handle* h, int nsteps) {
         if (e2 != cudaSuccess) return fail(h, NS_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e2));
       }
       NS_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+      h->launches += h->graph_launches;
     }
     h->first_pending = false;
     h->steps++;
   }
+  return NS_OK;
+}
+
+int ns_launch_count(const ns_handle* h, long long* launches) {
+  if (!h || !launches) return NS_ERR_ARG;
+  *launches = h->launches;
+  return NS_OK;
+}
+
+int ns_profile(ns_handle* h, int nsteps, ns_kernel_time* out, int max_out, int* n_out) {
+  if (!h || !out || !n_out || nsteps < 1 || max_out < 1) return NS_ERR_ARG;
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  cudaEvent_t start;
+  NS_CUDA(h, cudaEventCreate(&start));
+  NS_CUDA(h, cudaEventRecord(start, h->stream));
+  h->profiling = true;
+  int s = NS_OK;
+  for (int it = 0; it < nsteps && s == NS_OK; ++it) {
+    const bool first = h->first_pending && h->cfg.scheme != NS_EULER;
+    s = enqueue_step(h, first);
+    h->first_pending = false;
+    h->steps++;
+  }
+  h->profiling = false;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  int n = 0;
+  cudaEvent_t prev = start;
+  for (auto& pe : h->prof_events) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, prev, pe.second);
+    int slot = -1;
+    for (int q = 0; q < n; ++q)
+      if (pe.first == out[q].name) slot = q;
+    if (slot < 0 && n < max_out) {
+      slot = n++;
+      std::memset(&out[slot], 0, sizeof(out[slot]));
+      std::strncpy(out[slot].name, pe.first.c_str(), sizeof(out[slot].name) - 1);
+    }
+    if (slot >= 0) {
+      out[slot].ms += ms;
+      out[slot].launches += 1;
+    }
+    prev = pe.second;
+  }
+  for (auto& pe : h->prof_events) cudaEventDestroy(pe.second);
+  h->prof_events.clear();
+  cudaEventDestroy(start);
+  *n_out = n;
+  if (s) return s;
+  if (e != cudaSuccess) return fail(h, NS_ERR_CUDA, cudaGetErrorString(e));
   return NS_OK;
 }
 

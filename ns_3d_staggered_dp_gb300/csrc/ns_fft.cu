@@ -531,29 +531,35 @@ bool fft_size_supported(int nx, int ny, int nz) {
   return ok(nx) && ok(ny) && ok(nz);
 }
 
-cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* /*rhs_tmp*/, double* dp,
-                               const Layout& L, cudaStream_t st) {
+cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk) {
   const FOne c{d.one, d.mzero};
   cudaError_t e = cudaSuccess;
 #define X_FWD(n) e = launch_x_fwd<(n) / 2>(P, d, spec, st)
   NS_SIZE_SWITCH(P.nx, X_FWD)
 #undef X_FWD
   if (e != cudaSuccess) return e;
+  mk("fft_x_fwd");
 #define Y_FWD(n) e = launch_y<(n), -1>(P, spec, c, st)
   NS_SIZE_SWITCH(P.ny, Y_FWD)
 #undef Y_FWD
   if (e != cudaSuccess) return e;
+  mk("fft_y_fwd");
 #define Z_SOL(n) e = launch_z<(n)>(P, spec, c, st)
   NS_SIZE_SWITCH(P.nz, Z_SOL)
 #undef Z_SOL
   if (e != cudaSuccess) return e;
+  mk("fft_z_solve");
 #define Y_INV(n) e = launch_y<(n), 1>(P, spec, c, st)
   NS_SIZE_SWITCH(P.ny, Y_INV)
 #undef Y_INV
   if (e != cudaSuccess) return e;
+  mk("fft_y_inv");
 #define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st)
   NS_SIZE_SWITCH(P.nx, X_INV)
 #undef X_INV
+  if (e != cudaSuccess) return e;
+  mk("fft_x_inv");
   return e;
 }
 

@@ -4,6 +4,16 @@
 
 namespace ns {
 
+// Called after every kernel launch with the kernel's name (launch counting
+// and per-kernel event timing in ns_api.cu).
+struct Marker {
+  void (*fn)(void*, const char*) = nullptr;
+  void* ctx = nullptr;
+  void operator()(const char* name) const {
+    if (fn) fn(ctx, name);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Predictor (ns_predict.cu)
 // ---------------------------------------------------------------------------
@@ -132,8 +142,8 @@ struct DivArgs {
   double one, mzero;
   const double* rhs;     // non-null: transform this right-hand side (cell slots) instead of div(u*)/dt
 };
-cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* rhs_tmp, double* dp,
-                               const Layout& L, cudaStream_t st);
+cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)

@@ -49,7 +49,12 @@ def tgv_state(cfg, seed=1234, noise=1e-3):
     st.u = st.u + rng.uniform(-noise, noise, st.u.shape)
     st.v = st.v + rng.uniform(-noise, noise, st.v.shape)
     st.w = st.w + rng.uniform(-noise, noise, st.w.shape)
-    faces = O.Faces.zeros(nx, ny, nz)
+    return project(st, cfg)
+
+
+def project(st, cfg):
+    """Make the velocity discretely divergence-free with the oracle's Poisson solve."""
+    faces = O.Faces.zeros(cfg.nx, cfg.ny, cfg.nz)
     O.vel_bc_staggered(st.u, st.v, st.w, faces, *cfg.bc)
     dx, dy, dz = cfg.h
     I = slice(1, -1)
