@@ -1,6 +1,7 @@
 // C ABI of libns_gpu.so: sessions, state transfer, boundary faces, the time
 // step and the routine tier.  See include/ns_gpu.h for the contract and the
 // reference routine each entry point replaces.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -133,6 +134,7 @@ struct ns_handle {
   double *u = nullptr, *v = nullptr, *w = nullptr, *p = nullptr;
   double *hx = nullptr, *hy = nullptr, *hz = nullptr;
   double *us = nullptr, *vs = nullptr, *ws = nullptr, *dp = nullptr;
+  double *us2 = nullptr, *vs2 = nullptr, *ws2 = nullptr;  // ADI ping-pong buffers
   double2* spec = nullptr;
   double* inv_lam = nullptr;
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
@@ -308,25 +310,34 @@ PredictArgs predict_args(ns_handle* h) {
   return a;
 }
 
+// The three sweeps with fixed buffer roles: x reads A (the predictor's
+// output) and writes B, y reads B and writes A, z reads A and writes B, so
+// the final u*, v*, w* are in B on every step (and in every captured graph).
 int enqueue_adi(ns_handle* h) {
-  const ns_config& c = h->cfg;
+  double* A[3] = {h->us, h->vs, h->ws};
+  double* B[3] = {h->us2, h->vs2, h->ws2};
   for (int ax = 0; ax < 3; ++ax) {
     AdiArgs a{};
     a.L = h->L;
-    a.f[0] = h->us; a.f[1] = h->vs; a.f[2] = h->ws;
     for (int f = 0; f < 3; ++f) {
+      a.src[f] = (ax == 1) ? B[f] : A[f];
+      a.dst[f] = (ax == 1) ? A[f] : B[f];
       a.sys[f] = h->sys[ax][f];
       a.face_lo[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][0] : nullptr;
       a.face_hi[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][1] : nullptr;
-      const int n1 = plane_n1(h->L, ax), n2 = plane_n2(h->L, ax);
-      a.ext_lo[f][0] = 0; a.ext_lo[f][1] = 0;
-      a.ext_hi[f][0] = n1 - 1; a.ext_hi[f][1] = n2 - 1;
     }
-    (void)c;
     NS_CUDA(h, launch_adi(ax, a, h->stream));
     mark(h, ax == 0 ? "adi_x" : (ax == 1 ? "adi_y" : "adi_z"));
   }
   return NS_OK;
+}
+
+// u*, v*, w* after the explicit predictor + BC fill or after the ADI sweeps.
+inline void final_star(ns_handle* h, const double** fs) {
+  const bool cn = h->cfg.scheme == NS_AB2_CN;
+  fs[0] = cn ? h->us2 : h->us;
+  fs[1] = cn ? h->vs2 : h->vs;
+  fs[2] = cn ? h->ws2 : h->ws;
 }
 
 int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
@@ -334,7 +345,9 @@ int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
   DivArgs d{};
   d.rhs = rhs;
   d.L = h->L;
-  d.us = h->us; d.vs = h->vs; d.ws = h->ws;
+  const double* fs[3];
+  final_star(h, fs);
+  d.us = fs[0]; d.vs = fs[1]; d.ws = fs[2];
   d.cdx = 1.0 / (h->dx * c.dt); d.cdy = 1.0 / (h->dy * c.dt); d.cdz = 1.0 / (h->dz * c.dt);
   d.one = 1.0; d.mzero = -0.0;
   NS_CUDA(h, launch_fft_poisson(h->plan, d, h->spec, h->dp, h->L, h->stream, marker(h)));
@@ -359,7 +372,9 @@ int enqueue_step(ns_handle* h, bool first) {
   if (s) return s;
   CorrectArgs ca{};
   ca.L = h->L;
-  ca.us = h->us; ca.vs = h->vs; ca.ws = h->ws; ca.dp = h->dp;
+  const double* fs[3];
+  final_star(h, fs);
+  ca.us = fs[0]; ca.vs = fs[1]; ca.ws = fs[2]; ca.dp = h->dp;
   ca.u = h->u; ca.v = h->v; ca.w = h->w; ca.p = h->p;
   ca.gx = -c.dt / h->dx; ca.gy = -c.dt / h->dy; ca.gz = -c.dt / h->dz;
   ca.dp_flag = c.dp_flag; ca.gauge = c.gauge;
@@ -415,6 +430,8 @@ int build_plans(ns_handle* h) {
   return NS_OK;
 }
 
+constexpr int kAdiPad = 8;  // zero padding on each side of the factor tables
+
 int build_adi(ns_handle* h) {
   const ns_config& c = h->cfg;
   if (c.scheme != NS_AB2_CN) return NS_OK;
@@ -425,22 +442,22 @@ int build_adi(ns_handle* h) {
   for (int ax = 0; ax < 3; ++ax)
     for (int f = 0; f < 3; ++f) {
       hs_sys[ax][f] = build_cn_system(ns_[ax], c.bc[ax], hs[ax], c.dt, c.nu, f == ax, c.cn_periodic_closure);
-      total += hs_sys[ax][f].l.size() * 3 + hs_sys[ax][f].z.size();
+      total += (hs_sys[ax][f].l.size() + 2 * kAdiPad) * 3 + hs_sys[ax][f].z.size();
     }
   NS_CUDA(h, cudaMalloc(&h->adi_buf, total * sizeof(double)));
-  std::vector<double> host(total);
+  std::vector<double> host(total, 0.0);
   size_t off = 0;
   for (int ax = 0; ax < 3; ++ax)
     for (int f = 0; f < 3; ++f) {
       const HostLineSys& S = hs_sys[ax][f];
       LineSys& D = h->sys[ax][f];
-      const size_t m = S.l.size();
-      std::memcpy(&host[off], S.l.data(), m * sizeof(double)); D.l = h->adi_buf + off; off += m;
-      std::memcpy(&host[off], S.dinv.data(), m * sizeof(double)); D.dinv = h->adi_buf + off; off += m;
-      std::memcpy(&host[off], S.cu.data(), m * sizeof(double)); D.cu = h->adi_buf + off; off += m;
+      const size_t m = S.l.size(), mp = m + 2 * kAdiPad;
+      std::memcpy(&host[off + kAdiPad], S.l.data(), m * sizeof(double)); D.l = h->adi_buf + off; off += mp;
+      std::memcpy(&host[off + kAdiPad], S.dinv.data(), m * sizeof(double)); D.dinv = h->adi_buf + off; off += mp;
+      std::memcpy(&host[off + kAdiPad], S.cu.data(), m * sizeof(double)); D.cu = h->adi_buf + off; off += mp;
       std::memcpy(&host[off], S.z.data(), S.z.size() * sizeof(double)); D.z = h->adi_buf + off; off += S.z.size();
       D.s0 = S.s0; D.s1 = S.s1; D.zA = S.zA; D.zB = S.zB; D.lo = S.lo; D.hi = S.hi;
-      D.periodic = S.periodic; D.n = S.n;
+      D.periodic = S.periodic; D.n = S.n; D.pad = kAdiPad;
     }
   NS_CUDA(h, cudaMemcpyAsync(h->adi_buf, host.data(), total * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -449,7 +466,8 @@ int build_adi(ns_handle* h) {
 
 void free_all(ns_handle* h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
-  double* bufs[] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz, h->us, h->vs, h->ws, h->dp, h->inv_lam, h->adi_buf, h->face_buf};
+  double* bufs[] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz, h->us, h->vs, h->ws, h->dp, h->inv_lam, h->adi_buf, h->face_buf,
+                    h->us2, h->vs2, h->ws2};
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (h->spec) cudaFree(h->spec);
@@ -511,7 +529,8 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(NS_ERR_CUDA);
   h->own_stream = true;
   if (cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(NS_ERR_CUDA);
-  double** fields[] = {&h->u, &h->v, &h->w, &h->p, &h->hx, &h->hy, &h->hz, &h->us, &h->vs, &h->ws, &h->dp};
+  double** fields[] = {&h->u, &h->v, &h->w, &h->p, &h->hx, &h->hy, &h->hz, &h->us, &h->vs, &h->ws, &h->dp,
+                       &h->us2, &h->vs2, &h->ws2};
   for (double** f : fields) {
     if (cudaMalloc(f, h->L.fsize * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
     if (cudaMemsetAsync(*f, 0, h->L.fsize * sizeof(double), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
@@ -841,9 +860,9 @@ int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star) {
   NS_CUDA(h, h2d_field(h, h->ws, w_star, 2));
   int s = enqueue_adi(h);
   if (s) return s;
-  NS_CUDA(h, d2h_field(h, u_star, h->us, 0));
-  NS_CUDA(h, d2h_field(h, v_star, h->vs, 1));
-  NS_CUDA(h, d2h_field(h, w_star, h->ws, 2));
+  NS_CUDA(h, d2h_field(h, u_star, h->us2, 0));
+  NS_CUDA(h, d2h_field(h, v_star, h->vs2, 1));
+  NS_CUDA(h, d2h_field(h, w_star, h->ws2, 2));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
   return NS_OK;
 }

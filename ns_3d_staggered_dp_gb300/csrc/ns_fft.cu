@@ -104,22 +104,42 @@ __device__ __forceinline__ void bfly(double2& a, double2& b, int q, const FOne& 
 }
 
 // In-place R-point DFT (R a power of two, R <= 32), natural order in and out.
+// Every index is a template constant, so the array stays in registers.
+template <int R, int I>
+struct BitRev {
+  static __device__ __forceinline__ void run(double2 (&x)[R]) {
+    constexpr int J = brevc(I, ilog2c(R));
+    if constexpr (J > I) {
+      const double2 t = x[I];
+      x[I] = x[J];
+      x[J] = t;
+    }
+    BitRev<R, I + 1>::run(x);
+  }
+};
+template <int R>
+struct BitRev<R, R> {
+  static __device__ __forceinline__ void run(double2 (&)[R]) {}
+};
+template <int R, int LEN, int S, int K, int DIR>
+struct Bfly {  // butterfly K of group S of stage LEN, then the next one
+  static __device__ __forceinline__ void run(double2 (&x)[R], const FOne& c) {
+    bfly<DIR>(x[S + K], x[S + K + LEN / 2], K * (32 / LEN), c);
+    if constexpr (K + 1 < LEN / 2) Bfly<R, LEN, S, K + 1, DIR>::run(x, c);
+    else if constexpr (S + LEN < R) Bfly<R, LEN, S + LEN, 0, DIR>::run(x, c);
+  }
+};
+template <int R, int LEN, int DIR>
+struct Stage {
+  static __device__ __forceinline__ void run(double2 (&x)[R], const FOne& c) {
+    Bfly<R, LEN, 0, 0, DIR>::run(x, c);
+    if constexpr (LEN < R) Stage<R, 2 * LEN, DIR>::run(x, c);
+  }
+};
 template <int R, int DIR>
 __device__ __forceinline__ void dft(double2 (&x)[R], const FOne& c) {
-  constexpr int B = ilog2c(R);
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int j = brevc(i, B);
-    if (j > i) { const double2 tmp = x[i]; x[i] = x[j]; x[j] = tmp; }
-  }
-#pragma unroll
-  for (int len = 2; len <= R; len <<= 1) {
-#pragma unroll
-    for (int s = 0; s < R; s += len) {
-#pragma unroll
-      for (int k = 0; k < len / 2; ++k) bfly<DIR>(x[s + k], x[s + k + len / 2], k * (32 / len), c);
-    }
-  }
+  BitRev<R, 0>::run(x);
+  Stage<R, 2, DIR>::run(x, c);
 }
 
 __device__ __forceinline__ double2 cmul(const FOne& c, double2 a, double2 w) {
@@ -149,11 +169,14 @@ template <> struct Split<512> { static constexpr int R1 = 16, R2 = 32; };
 // y / z passes: lanes over consecutive kx (coalesced), T threads per line.
 // Shared buffer index for line l: (r * R2 + q) * LPC + l.
 // ---------------------------------------------------------------------------
-constexpr int LPC = 16;
+// Lines per CTA: 8 for the long lines (register-heavy 16-point DFTs), else 16.
+template <int N>
+constexpr int lpc() { return N >= 256 ? 8 : 16; }
 
 template <int N>
 struct YZ {
   static constexpr int R1 = Split<N>::R1, R2 = Split<N>::R2, T = R1, KQ = R2 / T;
+  static constexpr int LPC = lpc<N>();
   __device__ static __forceinline__ int sidx(int r, int q, int l) { return (r * R2 + q) * LPC + l; }
 
   // Forward step A: thread n1 = t loads x[n1 + R1 n2], R2-point DFT, twiddle, to smem (n1, k2).
@@ -209,10 +232,10 @@ struct LineGeo {
   long long base;
   bool valid;
 };
-__device__ __forceinline__ int yz_nblk(int nxh) { return (nxh - 1 + LPC - 1) / LPC; }
-__device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, int l) {
+__host__ __device__ __forceinline__ int yz_nblk(int nxh, int LPC) { return (nxh - 1 + LPC - 1) / LPC; }
+__device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, int l, int LPC) {
   const int M = nxh - 1;
-  const int nblk = yz_nblk(nxh);
+  const int nblk = yz_nblk(nxh, LPC);
   LineGeo G;
   int kx, o;
   if ((int)blockIdx.x < nblk) {
@@ -232,13 +255,14 @@ __device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, in
 }
 
 template <int N, int DIR>
-__global__ void __launch_bounds__(LPC * Split<N>::R1) fft_y_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_y_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
   using F = YZ<N>;
+  constexpr int LPC = F::LPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* sb = reinterpret_cast<double2*>(smem_raw);
   const int l = threadIdx.x, t = threadIdx.y;
-  const LineGeo G = yz_line(1, P.nxh, P.ny, P.nz, l);
-  if ((int)blockIdx.x == yz_nblk(P.nxh) && blockIdx.y * LPC >= (unsigned)P.nz) return;  // whole block idle
+  const LineGeo G = yz_line(1, P.nxh, P.ny, P.nz, l, LPC);
+  if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && blockIdx.y * LPC >= (unsigned)P.nz) return;  // whole block idle
   double2* g = spec + G.base;
   const long long st = P.nxh;
   if (DIR < 0) {
@@ -266,13 +290,14 @@ __global__ void __launch_bounds__(LPC * Split<N>::R1) fft_y_kernel(FftPlan P, do
 }
 
 template <int N>
-__global__ void __launch_bounds__(LPC * Split<N>::R1) fft_z_solve_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_z_solve_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
   using F = YZ<N>;
+  constexpr int LPC = F::LPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* sb = reinterpret_cast<double2*>(smem_raw);
   const int l = threadIdx.x, t = threadIdx.y;
-  if ((int)blockIdx.x == yz_nblk(P.nxh) && blockIdx.y * LPC >= (unsigned)P.ny) return;
-  const LineGeo G = yz_line(2, P.nxh, P.ny, P.nz, l);
+  if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && blockIdx.y * LPC >= (unsigned)P.ny) return;
+  const LineGeo G = yz_line(2, P.nxh, P.ny, P.nz, l, LPC);
   double2* g = spec + G.base;
   const double* lam = P.inv_lam + G.base;
   const long long st = (long long)P.nxh * P.ny;
@@ -467,7 +492,7 @@ __global__ void __launch_bounds__(256) fft_x_inv_kernel(FftPlan P, const double2
 template <int M>
 size_t xp_smem() { return (size_t)XP<M>::LINES * XP<M>::LS * sizeof(double2); }
 template <int N>
-size_t yz_smem() { return (size_t)N * LPC * sizeof(double2); }
+size_t yz_smem() { return (size_t)N * lpc<N>() * sizeof(double2); }
 
 template <int M>
 cudaError_t launch_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st) {
@@ -495,8 +520,8 @@ cudaError_t launch_y(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
   const size_t sm = yz_smem<N>();
   cudaError_t e = cudaFuncSetAttribute(fft_y_kernel<N, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  const int M = P.nxh - 1;
-  dim3 grid((M + LPC - 1) / LPC + 1, P.nz);
+  constexpr int LPC = lpc<N>();
+  dim3 grid(yz_nblk(P.nxh, LPC) + 1, P.nz);
   dim3 block(LPC, Split<N>::R1);
   fft_y_kernel<N, DIR><<<grid, block, sm, st>>>(P, spec, c);
   return cudaGetLastError();
@@ -506,8 +531,8 @@ cudaError_t launch_z(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
   const size_t sm = yz_smem<N>();
   cudaError_t e = cudaFuncSetAttribute(fft_z_solve_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  const int M = P.nxh - 1;
-  dim3 grid((M + LPC - 1) / LPC + 1, P.ny);
+  constexpr int LPC = lpc<N>();
+  dim3 grid(yz_nblk(P.nxh, LPC) + 1, P.ny);
   dim3 block(LPC, Split<N>::R1);
   fft_z_solve_kernel<N><<<grid, block, sm, st>>>(P, spec, c);
   return cudaGetLastError();

@@ -102,23 +102,24 @@ cudaError_t launch_pr_bc(const Layout& L, double* dp, const FaceSet& F, const in
 // ---------------------------------------------------------------------------
 // Factors of one line system (same for every line of a sweep and field).
 struct LineSys {
-  const double* l;     // forward multipliers, length n_unk
-  const double* dinv;  // 1/pivot
-  const double* cu;    // super-diagonal * dinv
-  const double* z;     // Sherman-Morrison vector (periodic only)
+  const double* l;     // forward multipliers; index pad + e for unknown e, zero-padded
+  const double* dinv;  // 1/pivot (zero in the padding)
+  const double* cu;    // super-diagonal * dinv (zero in the padding)
+  const double* z;     // Sherman-Morrison vector (periodic only), index e
   double s0, s1;       // correction weights of y[first] and y[last] (periodic only)
   int zA, zB;          // the correction is applied on [0, zA) and [zB, n_unk)
   int lo, hi;          // first/last unknown slot along the axis
   int periodic;        // 1: reduced cyclic system on slots 1..n + copies to slots 0, n+1
   int n;               // cells along the axis
+  int pad;             // zero padding on each side of the factor tables
 };
 struct AdiArgs {
   Layout L;
-  double* f[3];          // u*, v*, w*
+  const double* src[3];  // u*, v*, w* before the sweep
+  double* dst[3];        // after the sweep (another buffer: fixed ping-pong roles)
   LineSys sys[3];        // per field (normal or tangential system)
   const double* face_lo[3];  // BC row values per field (internal-slot planes), NULL -> 0
   const double* face_hi[3];
-  int ext_lo[3][2], ext_hi[3][2];  // line-index ranges in the two other axes, per field
 };
 cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st);
 

@@ -13,10 +13,12 @@
 //
 // Tiling: a CTA owns 32 x-cells by TY y-rows and marches along z through a
 // chunk of KC planes.  Warp w (0..TY) is y-row j0-1+w; warp 0 only computes
-// the products of the low y-halo row.  Products are owned one-sided (cell a
-// owns SX[a], and the face products at faces a+1), so an output cell needs
-// products of its own and its lower neighbours only; lane 0's low x-halo
-// products are computed by a single lane (8 FP64 ops per row and plane).
+// products: those of the low y-halo row and, in one extra pass with lane r
+// on row r, the low x-halo position of every row.  Products are owned
+// one-sided (cell a owns SX[a], and the face products at faces a+1), so an
+// output cell needs products of its own and its lower neighbours only.  An
+// FP64 warp instruction costs its full issue slot however many lanes are
+// active, so no halo work is done by single lanes of the row warps.
 // Every FP64 operation is issued in FMA form (see ns_internal.cuh).
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
@@ -26,8 +28,8 @@ namespace ns {
 namespace {
 
 constexpr int TX = 32;
-constexpr int TY = 8;
-constexpr int KC = 32;
+constexpr int TY = 16;
+constexpr int KC = 16;
 constexpr int SXW = TX + 2;  // smem row width: x in [i0-1, i0+32]
 constexpr int SYH = TY + 2;  // smem rows: y in [j0-1, j0+TY]
 constexpr int PXW = TX + 1;  // product row width: x in [i0-1, i0+31]
@@ -133,7 +135,8 @@ __global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
   __syncthreads();
   if (MODE != 2) {
     products_zface(S, c, xa, yb, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
-    if (lane == 0) products_zface(S, c, 0, yb, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
+    // low x-halo position of every row, by warp 0 (one partially active pass)
+    if (wy == 0 && lane <= TY) products_zface(S, c, 0, lane, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
   }
 
   const int i = i0 + lane;
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
     __syncthreads();
     if (MODE != 2) {
       products(S, c, xa, yb, s0, s1, pb);
-      if (lane == 0) products(S, c, 0, yb, s0, s1, pb);
+      if (wy == 0 && lane <= TY) products(S, c, 0, lane, s0, s1, pb);
     }
     __syncthreads();
     const bool act_w = (k >= a.wlo);
