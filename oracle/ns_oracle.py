@@ -20,8 +20,11 @@ cosine/sine transforms by ``scipy.fft.dct/dst`` with the MKL normalisation
 written out in ``mkl_tt_*``; the dense LU by ``scipy.linalg.lu_factor``; the
 sparse LU by ``scipy.sparse.linalg.splu``.
 
-Parity pinning: the reference has no golden vectors for this path (its
-``test_subroutine.f90`` only prints).  The oracle is pinned by (i) the
+Parity unpinned: no output of the reference itself pins this restatement.
+The reference cannot be built here (Fortran + Intel MKL + HDF5; no Fortran
+compiler or MKL on either machine), its ``test_subroutine.f90`` only prints,
+and its ``err_file/`` logs come from a JHTDB-initialised run whose data is
+not in the repository.  In place of golden vectors the oracle is checked by (i) the
 reference's own bitwise check that the new and legacy stencil primitives
 agree (test_subroutine.f90:137-185), restated here as ``avg_old`` and friends;
 (ii) the spectral Poisson solves agreeing with a sparse LU solve of the
