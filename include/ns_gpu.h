@@ -156,6 +156,25 @@ int ns_poisson(ns_handle* h, const double* rhs, double* dp);
  * (big_periodic_3D.f90:425-489; re_simulation_sub_tstep_interBC_combine.f90:656-701). */
 int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star);
 
+/* The periodic FFT pressure Poisson solve of ns_poisson without any device
+ * allocation.  No counterpart in the reference: it serves callers that must
+ * not allocate device memory (code running under CUDA stream capture, hosts
+ * whose device memory is owned by another allocator, real-time loops that
+ * cannot take an allocation's device synchronisation).
+ *   rhs_dev: device array (nx, ny, nz), Fortran order, 16-byte aligned,
+ *            already BC-modified (periodic: none);
+ *   dp_dev : device array (nx+2, ny+2, nz+2), Fortran order; the interior is
+ *            the solution (zero mean) and the ghosts are the periodic copies;
+ *   stream : cudaStream_t the work is enqueued on (NULL: legacy stream).
+ * All scratch (half spectrum, twiddles, 1/lambda; 4 MiB) is one static
+ * device array held by every device that loads the library.  Grids are
+ * limited to powers of two in [16, 64] per axis (NS_ERR_SHAPE otherwise).
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race. */
+int ns_poisson_fft_noalloc(const double* rhs_dev, double* dp_dev, int nx, int ny, int nz, double lx, double ly,
+                           double lz, void* stream);
+
 /* ------------------------------------------------------------------------
  * Tracing (the per-phase SYSTEM_CLOCK prints of big_periodic_3D.f90:328-569).
  * ------------------------------------------------------------------------ */

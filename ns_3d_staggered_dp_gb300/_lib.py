@@ -61,6 +61,8 @@ SIGNATURES = {
     "ns_adi": (C.c_int, [C.c_void_p, _DP, _DP, _DP]),
     "ns_profile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(NSKernelTime), C.c_int, C.POINTER(C.c_int)]),
     "ns_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "ns_poisson_fft_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                         C.c_double, C.c_void_p]),
     "ns_version": (C.c_char_p, []),
 }
 

@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(256) fft_x_fwd_kernel(FftPlan P, DivArgs d, do
   }
 }
 
-template <int M>
+template <int M, bool ALIGNED>
 __global__ void __launch_bounds__(256) fft_x_inv_kernel(FftPlan P, const double2* __restrict__ spec, double* dp,
                                                         Layout L, FOne c) {
   using X = XP<M>;
@@ -483,7 +483,12 @@ __global__ void __launch_bounds__(256) fft_x_inv_kernel(FftPlan P, const double2
 #pragma unroll
       for (int b = 0; b < R2; ++b) {
         const int m = t + R1 * b;
-        *reinterpret_cast<double2*>(o + 2 * m + 1) = x[b];
+        if (ALIGNED) {
+          *reinterpret_cast<double2*>(o + 2 * m + 1) = x[b];
+        } else {
+          o[2 * m + 1] = x[b].x;
+          o[2 * m + 2] = x[b].y;
+        }
       }
     }
   }
@@ -508,11 +513,12 @@ cudaError_t launch_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cuda
 template <int M>
 cudaError_t launch_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, FOne c, cudaStream_t st) {
   const size_t sm = xp_smem<M>();
-  cudaError_t e = cudaFuncSetAttribute(fft_x_inv_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  auto kern = P.dp_unaligned ? fft_x_inv_kernel<M, false> : fft_x_inv_kernel<M, true>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   const int lines = L.ny * L.nz;
   dim3 block(XP<M>::T, XP<M>::LINES);
-  fft_x_inv_kernel<M><<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, spec, dp, L, c);
+  kern<<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, spec, dp, L, c);
   return cudaGetLastError();
 }
 template <int N, int DIR>

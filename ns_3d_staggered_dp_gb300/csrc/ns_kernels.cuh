@@ -133,6 +133,7 @@ struct FftPlan {
   const double2* tw_y;
   const double2* tw_z;
   const double* inv_lam;  // 1/(lambda * nx*ny*nz), (nxh, ny, nz), 0 at the mean mode
+  int dp_unaligned;       // 1: dp slot pairs (2m+1, 2m+2) are not 16-byte aligned (scalar stores)
 };
 struct DivArgs {
   Layout L;
