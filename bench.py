@@ -53,6 +53,14 @@ ALG_DOUBLES = {
     "correct": 8.0,       # read u*, v*, w*, dp; write u, v, w, p
 }
 
+# DRAM bytes per launch at 256^3 (dram__bytes_read.sum + dram__bytes_write.sum)
+# from one ncu capture of each kernel of this build's step.
+NCU_TRAFFIC_256 = {
+    "predict": 1649.1e6, "adi_x": 1469.8e6, "adi_y": 1588.6e6, "adi_z": 1588.6e6,
+    "fft_x_fwd": 533.7e6, "fft_y_fwd": 213.0e6, "fft_z_solve": 293.6e6, "fft_y_inv": 213.0e6,
+    "fft_x_inv": 219.9e6, "correct": 1112.1e6,
+}
+
 
 def hit_initial_field(n, k0=4.0, seed=2024):
     """Random-phase solenoidal field with E(k) ~ k^4 exp(-2 (k/k0)^2) on [0, 2pi]^3,
@@ -322,11 +330,7 @@ def run_ours(args):
     per_launch_ms = dms / max(1, dl)
     alg_bytes = ALG_DOUBLES.get(dname, 0.0) * 8.0 * ncell
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            traffic = json.load(f).get(dname)
+    traffic = NCU_TRAFFIC_256.get(dname) if n == 256 else None
     total_prof = sum(v[0] for v in prof.values())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
