@@ -11,10 +11,6 @@
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
 
-namespace ns {
-bool fft_size_supported(int nx, int ny, int nz);
-}
-
 using namespace ns;
 
 namespace {
@@ -255,11 +251,20 @@ int validate(const ns_config& c, std::string& msg) {
     if (c.pbc[a] < 1 || c.pbc[a] > 4) { msg = "pbc must be 1..4"; return NS_ERR_UNSUPPORTED_BC; }
     if ((c.bc[a] == 1) != (c.pbc[a] == 1)) { msg = "bc and pbc must agree on periodicity"; return NS_ERR_UNSUPPORTED_BC; }
   }
-  const bool allper = c.pbc[0] == 1 && c.pbc[1] == 1 && c.pbc[2] == 1;
-  if (!allper) { msg = "non-periodic pressure BCs need the DCT solver, not in this build"; return NS_ERR_UNSUPPORTED_BC; }
-  if (!ns::fft_size_supported(c.nx, c.ny, c.nz)) {
-    msg = "FFT sizes must be powers of two in [16, 512]";
-    return NS_ERR_SHAPE;
+  // Poisson: FFT on periodic axes, dense trigonometric transforms on the others.
+  if (c.pbc[0] != 1 && (c.pbc[1] == 1 || c.pbc[2] == 1)) {
+    msg = "a non-periodic x pressure axis needs non-periodic y and z as well";
+    return NS_ERR_UNSUPPORTED_BC;
+  }
+  auto pow2 = [](int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512; };
+  const int n3[3] = {c.nx, c.ny, c.nz};
+  for (int a = 0; a < 3; ++a) {
+    if (c.pbc[a] == 1 && !pow2(n3[a])) { msg = "FFT (periodic) axes must be powers of two in [16, 512]"; return NS_ERR_SHAPE; }
+    if (c.pbc[a] != 1 && a > 0 && n3[a] > 128) { msg = "non-periodic y/z axes are limited to 128 cells"; return NS_ERR_SHAPE; }
+    if (c.pbc[a] != 1 && a == 0 && (n3[a] % 2 != 0 || n3[a] > 1024)) {
+      msg = "a non-periodic x axis needs an even cell count <= 1024";
+      return NS_ERR_SHAPE;
+    }
   }
   if (!(c.dt > 0) || !(c.nu >= 0) || !(c.lx > 0) || !(c.ly > 0) || !(c.lz > 0)) { msg = "dt, nu, lengths"; return NS_ERR_ARG; }
   return NS_OK;
@@ -385,10 +390,67 @@ int enqueue_step(ns_handle* h, bool first) {
   return NS_OK;
 }
 
+// Dense transform pair of one non-periodic axis of n cells, from the MKL
+// trigonometric transforms DCT_poisson_solver applies (NS_functions.f90:1526-1625):
+//   pbc 3: F = backward staggered cosine (DCT-II / 2), G = forward staggered cosine
+//   pbc 2: sign flip of the odd (1-based) inputs, pbc-3 transform, reversal (and back)
+//   pbc 4: F = DST-I / 2 on n points, G = DST-I / (n + 1)
+// F[k][n'] (mode k from sample n'), G[n'][k] = F^-1, angles in long double.
+void dense_pair(int n, int pb, std::vector<double>& F, std::vector<double>& G) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  F.assign((size_t)n * n, 0.0);
+  G.assign((size_t)n * n, 0.0);
+  auto cosq = [&](long long m, long long q) {  // cos(pi m / q), m reduced mod 2q
+    m %= 2 * q;
+    return cosl(pi * (long double)m / (long double)q);
+  };
+  auto sinq = [&](long long m, long long q) {
+    m %= 2 * q;
+    return sinl(pi * (long double)m / (long double)q);
+  };
+  for (int k = 0; k < n; ++k)
+    for (int s = 0; s < n; ++s) {
+      long double f, g;
+      if (pb == 3 || pb == 2) {
+        const int kk = (pb == 2) ? n - 1 - k : k;  // reversal of the modes
+        const long double sg = (pb == 2 && s % 2 == 0) ? -1.0L : 1.0L;  // odd 1-based samples flipped
+        const long double cs = cosq((long long)kk * (2 * s + 1), 2LL * n);
+        f = sg * cs;
+        g = sg * cs * (kk == 0 ? 1.0L : 2.0L) / (long double)n;
+      } else {
+        const long double sn = sinq((long long)(k + 1) * (s + 1), n + 1);
+        f = sn;
+        g = 2.0L * sn / (long double)(n + 1);
+      }
+      F[(size_t)k * n + s] = (double)f;
+      G[(size_t)s * n + k] = (double)g;
+    }
+}
+
+// Eigenvalue sin^2(..)/h^2 of mode m (0-based) of one axis: FFT bins for pbc 1
+// (big_periodic_3D.f90:242-255), the trigonometric-transform modes otherwise
+// (re_simulation_sub_tstep_interBC_combine.f90:320-353).
+double axis_eig(int n, int pb, int m, double h) {
+  const double pi = 3.1415926535897932;
+  double s;
+  if (pb == 1) s = std::sin(pi * m / n);
+  else if (pb == 2) s = std::sin((m + 1) * pi / 2 / n);
+  else if (pb == 3) s = std::sin(m * pi / 2 / n);
+  else s = std::sin((m + 1) * pi / 2 / (n + 1));
+  return s * s / (h * h);
+}
+
 int build_plans(ns_handle* h) {
   const ns_config& c = h->cfg;
   const int nx = c.nx, ny = c.ny, nz = c.nz, M = nx / 2, nxh = M + 1;
-  // Twiddles W_N^m = exp(-2 pi i m / N), computed in long double.
+  const int n3[3] = {nx, ny, nz};
+  const double hs[3] = {h->dx, h->dy, h->dz};
+  FftPlan& P = h->plan;
+  P = FftPlan{};
+  for (int a = 0; a < 3; ++a) P.kind[a] = c.pbc[a] == 1 ? 0 : 1;
+  const bool xper = P.kind[0] == 0;
+  const int nxs = xper ? nxh : nx / 2;
+  // Twiddles W_N^m = exp(-2 pi i m / N), computed in long double (FFT axes only).
   auto twid = [](int N, int count, std::vector<double2>& out) {
     const long double pi = 3.141592653589793238462643383279502884L;
     for (int m = 0; m < count; ++m) {
@@ -397,36 +459,115 @@ int build_plans(ns_handle* h) {
     }
   };
   std::vector<double2> tw;
-  twid(M, M, tw);
-  const size_t o_xr = tw.size();
-  twid(nx, M / 2 + 1, tw);
-  const size_t o_y = tw.size();
-  twid(ny, ny, tw);
-  const size_t o_z = tw.size();
-  twid(nz, nz, tw);
+  size_t o_xr = 0, o_y = 0, o_z = 0;
+  if (xper) {
+    twid(M, M, tw);
+    o_xr = tw.size();
+    twid(nx, M / 2 + 1, tw);
+  }
+  o_y = tw.size();
+  if (P.kind[1] == 0) twid(ny, ny, tw);
+  o_z = tw.size();
+  if (P.kind[2] == 0) twid(nz, nz, tw);
+  if (tw.empty()) tw.push_back(make_double2(1.0, 0.0));
   NS_CUDA(h, cudaMalloc(&h->tw, tw.size() * sizeof(double2)));
   NS_CUDA(h, cudaMemcpyAsync(h->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
-  // Eigenvalues as big_periodic_3D.f90:242-255, inverted with the pipeline's scale.
-  const double pi = 3.1415926535897932;
-  std::vector<double> ex(nxh), ey(ny), ez(nz);
-  for (int i = 0; i < nxh; ++i) { const double s = std::sin(pi * i / nx) / h->dx; ex[i] = s * s; }
-  for (int i = 0; i < ny; ++i) { const double s = std::sin(pi * i / ny) / h->dy; ey[i] = s * s; }
-  for (int i = 0; i < nz; ++i) { const double s = std::sin(pi * i / nz) / h->dz; ez[i] = s * s; }
-  const double scale = 1.0 / (2.0 * (double)nx * (double)ny * (double)nz);
-  std::vector<double> il((size_t)nxh * ny * nz);
+  // Dense transform matrices: x stored transposed (F^T, G^T), y and z as is.
+  std::vector<double> dense;
+  size_t o_f[3] = {0, 0, 0}, o_g[3] = {0, 0, 0};
+  for (int a = 0; a < 3; ++a) {
+    if (P.kind[a] == 0) continue;
+    std::vector<double> F, G;
+    dense_pair(n3[a], c.pbc[a], F, G);
+    const int n = n3[a];
+    if (a == 0) {
+      std::vector<double> Ft((size_t)n * n), Gt((size_t)n * n);
+      for (int r = 0; r < n; ++r)
+        for (int q = 0; q < n; ++q) {
+          Ft[(size_t)q * n + r] = F[(size_t)r * n + q];
+          Gt[(size_t)q * n + r] = G[(size_t)r * n + q];
+        }
+      F.swap(Ft);
+      G.swap(Gt);
+    }
+    o_f[a] = dense.size();
+    dense.insert(dense.end(), F.begin(), F.end());
+    o_g[a] = dense.size();
+    dense.insert(dense.end(), G.begin(), G.end());
+  }
+  // Eigenvalues lambda = -4 (ex + ey + ez), inverted with the pipeline's
+  // scale: each FFT pass is unnormalised (x: 2 nx for the r2c/c2r pair), the
+  // dense pairs are exact inverses.
+  std::vector<double> e3[3];
+  for (int a = 0; a < 3; ++a) {
+    const int cnt = (a == 0 && xper) ? nxh : n3[a];
+    e3[a].resize(cnt);
+    for (int m = 0; m < cnt; ++m) e3[a][m] = axis_eig(n3[a], c.pbc[a], m, hs[a]);
+  }
+  double scale = 1.0;
+  if (xper) scale /= 2.0 * nx;
+  if (P.kind[1] == 0) scale /= ny;
+  if (P.kind[2] == 0) scale /= nz;
+  const bool allper = c.pbc[0] == 1 && c.pbc[1] == 1 && c.pbc[2] == 1;
+  bool singular = true;
+  for (int a = 0; a < 3; ++a) singular = singular && (c.pbc[a] == 1 || c.pbc[a] == 3);
+  // The singular mode: zero mean for the all-periodic FFT solve
+  // (big_periodic_3D.f90:242-255), mean_dp otherwise (NS_functions.f90:1576-1577).
+  P.has_mean = (singular && !allper) ? 1 : 0;
+  double dense_prod = 1.0;
+  for (int a = 0; a < 3; ++a)
+    if (P.kind[a] == 1) dense_prod *= n3[a];
+  P.mean_val = c.mean_dp * dense_prod;
+  const size_t nspec = (size_t)nxs * ny * nz;
+  auto inv_of = [&](int i, int j, int k) {
+    if (i == 0 && j == 0 && k == 0 && singular) return 0.0;
+    const double lam = -4.0 * ((e3[0][i] + e3[1][j]) + e3[2][k]);
+    return scale / lam;
+  };
+  std::vector<double> il;
+  std::vector<double2> il2;
+  if (P.kind[2] == 0) il.resize(nspec);
+  else il2.resize(nspec);
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j)
-      for (int i = 0; i < nxh; ++i) {
-        const double lam = -4.0 * ((ex[i] + ey[j]) + ez[k]);
-        il[i + (size_t)nxh * (j + (size_t)ny * k)] = (i == 0 && j == 0 && k == 0) ? 0.0 : scale / lam;
+      for (int i = 0; i < nxs; ++i) {
+        const size_t g = i + (size_t)nxs * (j + (size_t)ny * k);
+        if (P.kind[2] == 0) il[g] = inv_of(i, j, k);
+        else if (xper) il2[g] = make_double2(inv_of(i, j, k), inv_of(i, j, k));
+        else il2[g] = make_double2(inv_of(2 * i, j, k), inv_of(2 * i + 1, j, k));
       }
-  NS_CUDA(h, cudaMalloc(&h->inv_lam, il.size() * sizeof(double)));
-  NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, il.data(), il.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  // One buffer: 1/lambda table (double or double2), then the dense matrices.
+  const size_t n_il = il.empty() ? 2 * il2.size() : il.size();
+  const size_t n_dense = dense.size();
+  NS_CUDA(h, cudaMalloc(&h->inv_lam, (n_il + n_dense + 1) * sizeof(double)));
+  if (!il.empty())
+    NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, il.data(), il.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  else
+    NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, il2.data(), il2.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+  double* dbase = h->inv_lam + n_il;
+  if (n_dense)
+    NS_CUDA(h, cudaMemcpyAsync(dbase, dense.data(), n_dense * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
-  NS_CUDA(h, cudaMalloc(&h->spec, (size_t)nxh * ny * nz * sizeof(double2)));
-  h->plan.nx = nx; h->plan.ny = ny; h->plan.nz = nz; h->plan.nxh = nxh;
-  h->plan.tw_x = h->tw; h->plan.tw_xr = h->tw + o_xr; h->plan.tw_y = h->tw + o_y; h->plan.tw_z = h->tw + o_z;
-  h->plan.inv_lam = h->inv_lam;
+  NS_CUDA(h, cudaMalloc(&h->spec, nspec * sizeof(double2)));
+  P.nx = nx; P.ny = ny; P.nz = nz; P.nxh = nxh; P.nxs = nxs;
+  P.tw_x = h->tw; P.tw_xr = h->tw + o_xr; P.tw_y = h->tw + o_y; P.tw_z = h->tw + o_z;
+  P.inv_lam = il.empty() ? nullptr : h->inv_lam;
+  P.inv_lam2 = il.empty() ? reinterpret_cast<const double2*>(h->inv_lam) : nullptr;
+  for (int a = 0; a < 3; ++a) {
+    P.fwd[a] = P.kind[a] ? dbase + o_f[a] : nullptr;
+    P.inv[a] = P.kind[a] ? dbase + o_g[a] : nullptr;
+  }
+  // pr_bc_staggered_modify_rhs coefficients (NS_functions.f90:1345-1400) and
+  // the set-0 pressure face planes they read.
+  for (int a = 0; a < 3; ++a) {
+    const double hh = hs[a];
+    P.mod_lo[a] = P.mod_hi[a] = 0.0;
+    if (c.pbc[a] == 2) { P.mod_lo[a] = -2.0 / (hh * hh); P.mod_hi[a] = -2.0 / (hh * hh); }
+    else if (c.pbc[a] == 3) { P.mod_lo[a] = 1.0 / hh; P.mod_hi[a] = -1.0 / hh; }
+    else if (c.pbc[a] == 4) { P.mod_lo[a] = -1.0 / (hh * hh); P.mod_hi[a] = -1.0 / (hh * hh); }
+    P.face_lo[a] = h->faces[0].ax[a].f[3][0];
+    P.face_hi[a] = h->faces[0].ax[a].f[3][1];
+  }
   return NS_OK;
 }
 

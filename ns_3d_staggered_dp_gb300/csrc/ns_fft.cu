@@ -309,9 +309,12 @@ __global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_z_solve_kernel(Ff
   for (int q = 0; q < F::KQ; ++q)
 #pragma unroll
     for (int k1 = 0; k1 < F::R1; ++k1) {
-      const double s = G.valid ? __ldg(lam + (long long)(t + F::T * q + F::R2 * k1) * st) : 0.0;
+      const int kz = t + F::T * q + F::R2 * k1;
+      const double s = G.valid ? __ldg(lam + (long long)kz * st) : 0.0;
       xk[q][k1].x = fmul(c, xk[q][k1].x, s);
       xk[q][k1].y = fmul(c, xk[q][k1].y, s);
+      // singular mode of a Neumann/periodic mix: fixed mean (NS_functions.f90:1576-1577)
+      if (P.has_mean && G.valid && G.base == 0 && kz == 0) xk[q][k1] = make_double2(P.mean_val, 0.0);
     }
   __syncthreads();
   F::invA(xk, sb, P.tw_z, l, t, c);
@@ -333,7 +336,7 @@ struct XP {
   __device__ static __forceinline__ int sidx(int r, int q) { return r * ROW + q; }
 };
 
-template <int M, bool FROM_RHS>
+template <int M, bool FROM_RHS, bool HAS_BC>
 __global__ void __launch_bounds__(256) fft_x_fwd_kernel(FftPlan P, DivArgs d, double2* __restrict__ spec) {
   using X = XP<M>;
   constexpr int R1 = X::R1, R2 = X::R2, T = X::T, KQ = X::KQ;
@@ -377,6 +380,10 @@ __global__ void __launch_bounds__(256) fft_x_fwd_kernel(FftPlan P, DivArgs d, do
       double r1 = fmul(cc, fsub(cc, ub, ua.y), d.cdx);
       r1 = fma(fsub(cc, vb.y, va.y), d.cdy, r1);
       r1 = fma(fsub(cc, wb.y, wa.y), d.cdz, r1);
+      if (HAS_BC) {  // pr_bc_staggered_modify_rhs on the wall cells of y and z
+        r0 += P.bc_term(s, j, k);
+        r1 += P.bc_term(s + 1, j, k);
+      }
       x[n2] = make_double2(r0, r1);
     }
     dft<R2, -1>(x, cc);
@@ -502,7 +509,8 @@ size_t yz_smem() { return (size_t)N * lpc<N>() * sizeof(double2); }
 template <int M>
 cudaError_t launch_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st) {
   const size_t sm = xp_smem<M>();
-  auto kern = d.rhs ? fft_x_fwd_kernel<M, true> : fft_x_fwd_kernel<M, false>;
+  auto kern = d.rhs ? fft_x_fwd_kernel<M, true, false>
+                    : (P.any_bc_term() ? fft_x_fwd_kernel<M, false, true> : fft_x_fwd_kernel<M, false, false>);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   const int lines = d.L.ny * d.L.nz;
@@ -566,31 +574,57 @@ cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec
                                cudaStream_t st, const Marker& mk) {
   const FOne c{d.one, d.mzero};
   cudaError_t e = cudaSuccess;
+  // x forward: r2c FFT (periodic) or the dense transform with packed modes
+  if (P.kind[0] == 0) {
 #define X_FWD(n) e = launch_x_fwd<(n) / 2>(P, d, spec, st)
-  NS_SIZE_SWITCH(P.nx, X_FWD)
+    NS_SIZE_SWITCH(P.nx, X_FWD)
 #undef X_FWD
-  if (e != cudaSuccess) return e;
-  mk("fft_x_fwd");
+    if (e != cudaSuccess) return e;
+    mk("fft_x_fwd");
+  } else {
+    if ((e = launch_dense_x(true, P, d, spec, dp, L, st)) != cudaSuccess) return e;
+    mk("dense_x_fwd");
+  }
+  if (P.kind[1] == 0) {
 #define Y_FWD(n) e = launch_y<(n), -1>(P, spec, c, st)
-  NS_SIZE_SWITCH(P.ny, Y_FWD)
+    NS_SIZE_SWITCH(P.ny, Y_FWD)
 #undef Y_FWD
-  if (e != cudaSuccess) return e;
-  mk("fft_y_fwd");
+    if (e != cudaSuccess) return e;
+    mk("fft_y_fwd");
+  } else {
+    if ((e = launch_dense_yz(1, 0, P, spec, st)) != cudaSuccess) return e;
+    mk("dense_y_fwd");
+  }
+  if (P.kind[2] == 0) {
 #define Z_SOL(n) e = launch_z<(n)>(P, spec, c, st)
-  NS_SIZE_SWITCH(P.nz, Z_SOL)
+    NS_SIZE_SWITCH(P.nz, Z_SOL)
 #undef Z_SOL
-  if (e != cudaSuccess) return e;
-  mk("fft_z_solve");
+    if (e != cudaSuccess) return e;
+    mk("fft_z_solve");
+  } else {
+    if ((e = launch_dense_yz(2, 2, P, spec, st)) != cudaSuccess) return e;
+    mk("dense_z_solve");
+  }
+  if (P.kind[1] == 0) {
 #define Y_INV(n) e = launch_y<(n), 1>(P, spec, c, st)
-  NS_SIZE_SWITCH(P.ny, Y_INV)
+    NS_SIZE_SWITCH(P.ny, Y_INV)
 #undef Y_INV
-  if (e != cudaSuccess) return e;
-  mk("fft_y_inv");
+    if (e != cudaSuccess) return e;
+    mk("fft_y_inv");
+  } else {
+    if ((e = launch_dense_yz(1, 1, P, spec, st)) != cudaSuccess) return e;
+    mk("dense_y_inv");
+  }
+  if (P.kind[0] == 0) {
 #define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st)
-  NS_SIZE_SWITCH(P.nx, X_INV)
+    NS_SIZE_SWITCH(P.nx, X_INV)
 #undef X_INV
-  if (e != cudaSuccess) return e;
-  mk("fft_x_inv");
+    if (e != cudaSuccess) return e;
+    mk("fft_x_inv");
+  } else {
+    if ((e = launch_dense_x(false, P, d, spec, dp, L, st)) != cudaSuccess) return e;
+    mk("dense_x_inv");
+  }
   return e;
 }
 

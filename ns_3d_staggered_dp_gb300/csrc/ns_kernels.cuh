@@ -126,15 +126,50 @@ cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st);
 // ---------------------------------------------------------------------------
 // Periodic FFT Poisson (ns_fft.cu)
 // ---------------------------------------------------------------------------
+// Plan of the spectral pressure solve: per axis an FFT (periodic) or a dense
+// trigonometric transform pair (non-periodic, ns_dct.cu).
 struct FftPlan {
   int nx, ny, nz, nxh;
   const double2* tw_x;   // twiddles for the nx/2-point complex FFT (x)
   const double2* tw_xr;  // r2c split twiddles: exp(-2 pi i k / nx), k < nx/2
   const double2* tw_y;
   const double2* tw_z;
-  const double* inv_lam;  // 1/(lambda * nx*ny*nz), (nxh, ny, nz), 0 at the mean mode
+  const double* inv_lam;  // scale/lambda per spectrum entry (FFT z solve), 0 at the mean mode
   int dp_unaligned;       // 1: dp slot pairs (2m+1, 2m+2) are not 16-byte aligned (scalar stores)
+  int nxs;                // spectrum row length: nx/2+1 (periodic x) or nx/2 (packed wall x)
+  int kind[3];            // 0: FFT axis, 1: dense transform axis
+  const double* fwd[3];   // dense forward matrices (x: F^T [n][k]; y, z: F [k][n])
+  const double* inv[3];   // dense inverse matrices (x: G^T [k][n]; y, z: G [n][k])
+  const double2* inv_lam2;  // (re, im) scales of the dense z solve
+  int has_mean;           // 1: the singular mode is set to mean_val (after the forward passes)
+  double mean_val;
+  double mod_lo[3], mod_hi[3];        // pr_bc_staggered_modify_rhs coefficients per axis
+  const double* face_lo[3];           // pressure face planes per axis (internal slot order)
+  const double* face_hi[3];
+
+  // pr_bc_staggered_modify_rhs (NS_functions.f90:1345-1400) at interior cell (i, j, k).
+  __device__ __forceinline__ double bc_term(int i, int j, int k) const {
+    double t = 0.0;
+    const int n[3] = {nx, ny, nz};
+    const int idx[3] = {i, j, k};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      if (mod_lo[a] == 0.0 && mod_hi[a] == 0.0) continue;
+      const int s1 = (a == 0) ? j : i;
+      const int s2 = (a == 2) ? j : k;
+      const int n1 = (a == 0) ? ny + 2 : nx + 2;
+      const int pl = s1 + n1 * s2;
+      if (idx[a] == 1 && face_lo[a]) t = fma(mod_lo[a], face_lo[a][pl], t);
+      if (idx[a] == n[a] && face_hi[a]) t = fma(mod_hi[a], face_hi[a][pl], t);
+    }
+    return t;
+  }
+  __host__ __device__ bool any_bc_term() const {
+    return mod_lo[0] != 0.0 || mod_hi[0] != 0.0 || mod_lo[1] != 0.0 || mod_hi[1] != 0.0 || mod_lo[2] != 0.0 ||
+           mod_hi[2] != 0.0;
+  }
 };
+using SpecPlan = FftPlan;
 struct DivArgs {
   Layout L;
   const double* us;
@@ -144,8 +179,13 @@ struct DivArgs {
   double one, mzero;
   const double* rhs;     // non-null: transform this right-hand side (cell slots) instead of div(u*)/dt
 };
+// The spectral solve (FFT and dense axes mixed), divergence to dp interior.
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk);
+// Dense passes (ns_dct.cu): x forward/inverse; y/z mode 0 forward, 1 inverse, 2 (z) solve.
+cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                           cudaStream_t st);
+cudaError_t launch_dense_yz(int axis, int mode, const SpecPlan& S, double2* spec, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)

@@ -124,7 +124,7 @@ extern "C" int ns_poisson_fft_noalloc(const double* rhs_dev, double* dp_dev, int
   if (cudaGetLastError() != cudaSuccess) return NS_ERR_CUDA;
 
   FftPlan P{};
-  P.nx = nx; P.ny = ny; P.nz = nz; P.nxh = nxh;
+  P.nx = nx; P.ny = ny; P.nz = nz; P.nxh = nxh; P.nxs = nxh;
   P.tw_x = tw;
   P.tw_xr = tw + M;
   P.tw_y = tw + M + (M / 2 + 1);

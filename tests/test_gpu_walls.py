@@ -1,0 +1,186 @@
+"""Wall-bounded boxes on the CUDA path vs the CPU oracle, through the C ABI.
+
+Covers the non-periodic pressure solve (DCT_poisson_solver,
+NS_functions.f90:1505-1630, with pr_bc_staggered_modify_rhs :1345-1400 and
+pr_bc_staggered :1403-1464), its mix with periodic FFT axes, and full steps
+with wall velocity BCs (vel_bc_staggered :213-310, the banded CN-ADI of
+re_simulation_sub_tstep_interBC_combine.f90:656-701 with per-sweep faces).
+
+Tolerances: the dense trigonometric transforms round differently from the
+oracle's scipy DCT/DST, and the wall Poisson problem is less well
+conditioned than the periodic one, so the routine bound is a relative L2 of
+1e-11; full steps keep the 1e-10 per-field bound and max|div u| <= 1e-12.
+"""
+import numpy as np
+import pytest
+
+from oracle import ns_oracle as O
+from tests.helpers import random_state, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+POISSON_TOL = 1e-11
+STEP_TOL = 1e-10
+DIV_TOL = 1e-12
+
+
+def session(cfg, **kw):
+    from ns_3d_staggered_dp_gb300 import Session, make_config
+    return Session(make_config(cfg.nx, cfg.ny, cfg.nz, lx=cfg.lx, ly=cfg.ly, lz=cfg.lz, nu=cfg.nu, dt=cfg.dt,
+                               scheme=cfg.scheme, bc=cfg.bc, pbc=cfg.pbc, dp_flag=cfg.dp_flag, gauge=cfg.gauge,
+                               mean_dp=cfg.mean_dp, **kw))
+
+
+def random_faces(cfg, seed, amp=1.0):
+    rng = np.random.default_rng(seed)
+    shp = O.Faces.shapes(cfg.nx, cfg.ny, cfg.nz)
+    return O.Faces({k: amp * rng.standard_normal(s) for k, s in shp.items()})
+
+
+# (grid, pbc): every pure wall code, mixed wall codes, and the periodic/wall mixes
+POISSON_CASES = [
+    ((32, 16, 24), (3, 3, 3)),
+    ((32, 16, 24), (2, 2, 2)),
+    ((16, 24, 32), (4, 4, 4)),
+    ((24, 32, 16), (2, 3, 4)),
+    ((48, 24, 16), (3, 4, 2)),
+    ((32, 24, 16), (1, 3, 1)),
+    ((32, 16, 32), (1, 2, 1)),
+    ((16, 16, 32), (1, 4, 1)),
+    ((32, 32, 24), (1, 1, 3)),
+    ((16, 32, 16), (1, 1, 2)),
+    ((32, 24, 16), (1, 3, 3)),
+    ((64, 48, 24), (1, 2, 4)),
+]
+
+
+@pytest.mark.parametrize("grid,pbc", POISSON_CASES)
+def test_poisson_walls(grid, pbc):
+    nx, ny, nz = grid
+    singular = all(p in (1, 3) for p in pbc)
+    bc = tuple(1 if p == 1 else 2 for p in pbc)
+    cfg = O.Config(nx, ny, nz, lx=1.0, ly=0.8, lz=1.3, bc=bc, pbc=pbc, mean_dp=0.3 if singular else 0.0)
+    rng = np.random.default_rng(hash((grid, pbc)) % 2**32)
+    R = rng.standard_normal((nx, ny, nz))
+    faces = random_faces(cfg, 7)
+    dx, dy, dz = cfg.h
+    ref = np.zeros((nx + 2, ny + 2, nz + 2))
+    ref[1:-1, 1:-1, 1:-1] = O.poisson_solve(R, cfg, faces)
+    O.pr_bc_staggered(ref, faces, pbc, dx, dy, dz)
+    with session(cfg) as s:
+        s.set_faces(faces.d, 0)
+        got = s.poisson(R)
+    assert rel_l2(got, ref) < POISSON_TOL
+    # the interior solves the reference operator (the BC terms are in R already)
+    L = O.poisson_lhs_staggered(nx, ny, nz, dx * dx, dy * dy, dz * dz, pbc)
+    res = L @ got[1:-1, 1:-1, 1:-1].reshape(-1, order="F") - R.reshape(-1, order="F")
+    scale = np.abs(got).max() * 4.0 / min(dx, dy, dz) ** 2
+    if singular:  # the operator has a null space; compare against the mean-free residual
+        res = res - res.mean()
+    assert np.abs(res).max() < 1e-11 * scale
+    if singular:
+        assert abs(got[1:-1, 1:-1, 1:-1].mean() - cfg.mean_dp) < 1e-12
+
+
+def _run_compare(cfg, st, nsteps, faces=None, cn_faces=None, div_free=True, **kw):
+    ref = st.copy()
+    cnf = None
+    if cfg.scheme == O.AB2_CN:
+        dx, dy, dz = cfg.h
+        cnf = O.CNFactors(cfg.nx, cfg.ny, cfg.nz, cfg.bc, dx * dx, dy * dy, dz * dz, cfg.dt, cfg.nu)
+    with session(cfg, **kw) as s:
+        if faces is not None:
+            s.set_faces(faces.d, 0)
+        if cn_faces is not None:
+            for d in range(3):
+                s.set_faces(cn_faces[d].d, d + 1)
+        s.set_state(st.u, st.v, st.w, st.p, None if st.first else (st.px, st.py, st.pz))
+        umax = max(np.abs(st.u).max(), np.abs(st.v).max(), np.abs(st.w).max(), 1.0)
+        for _ in range(nsteps):
+            ref = O.step(ref, cfg, faces=faces, cn_faces=cn_faces, cnf=cnf)
+            s.step(1)
+            d = s.diag()
+            if div_free:
+                assert d["max_div"] < DIV_TOL * umax / min(cfg.h), d
+            else:  # incompatible Neumann data: the projection leaves mean(R) dt in every cell
+                ref_div = O.max_div(ref.u, ref.v, ref.w, *cfg.h)
+                assert abs(d["max_div"] - ref_div) < 1e-9 * max(ref_div, 1.0), (d, ref_div)
+        got = s.get_state()
+    for k, r in (("u", ref.u), ("v", ref.v), ("w", ref.w), ("p", ref.p), ("hx", ref.px), ("hy", ref.py),
+                 ("hz", ref.pz)):
+        err = rel_l2(got[k], r)
+        assert err < STEP_TOL, (k, err)
+    return got, ref
+
+
+def channel_state(cfg, seed=3, amp=0.05):
+    """Laminar parabolic profile in x between y walls plus a seeded
+    divergence-free perturbation (the small-box stand-in for the
+    256x128x256 wall-bounded configuration)."""
+    st = random_state(cfg, seed, amp=amp)
+    y = (np.arange(cfg.ny + 2) - 0.5) * cfg.ly / cfg.ny  # cell centres, ghosts included
+    prof = 4.0 * y * (cfg.ly - y) / cfg.ly ** 2
+    st.u = st.u + prof[None, :, None]
+    from tests.helpers import project
+    return project(st, cfg)
+
+
+@pytest.mark.parametrize("scheme", [O.EULER, O.AB2, O.AB2_CN])
+def test_step_channel(scheme):
+    """x, z periodic, y no-slip walls (bc 2) with Neumann pressure (pbc 3)."""
+    cfg = O.Config(32, 16, 32, lx=2 * np.pi, ly=2.0, lz=np.pi, nu=1.0 / 180, dt=2e-3, scheme=scheme,
+                   bc=(1, 2, 1), pbc=(1, 3, 1))
+    _run_compare(cfg, channel_state(cfg), 10)
+
+
+@pytest.mark.parametrize("scheme", [O.AB2, O.AB2_CN])
+@pytest.mark.parametrize("dp_flag", [0, 1])
+def test_step_open_box_faces(scheme, dp_flag):
+    """All-wall subdomain (bc 2, pbc 3) driven by random faces: a re-simulation
+    step with given boundary values, per-sweep ADI faces and a mean dp."""
+    cfg = O.Config(24, 16, 32, lx=0.75, ly=0.5, lz=1.0, nu=0.01, dt=1e-3, scheme=scheme, bc=(2, 2, 2),
+                   pbc=(3, 3, 3), dp_flag=dp_flag, mean_dp=0.05)
+    faces = random_faces(cfg, 11, amp=0.1)
+    cn_faces = [random_faces(cfg, 12 + d, amp=0.1) for d in range(3)] if scheme == O.AB2_CN else None
+    st = random_state(cfg, 5, amp=0.2)
+    # random faces carry a net flux that Neumann pressure data cannot remove
+    _run_compare(cfg, st, 6, faces=faces, cn_faces=cn_faces, div_free=False)
+
+
+@pytest.mark.parametrize("bc,pbc", [((4, 2, 4), (4, 2, 4)), ((2, 4, 2), (2, 3, 2)), ((2, 2, 4), (3, 2, 4))])
+def test_step_wall_codes(bc, pbc):
+    """Dirichlet-on-the-ghost (4) and Dirichlet-on-the-wall (2) codes mixed,
+    AB2-CN with per-sweep faces and the Euler start."""
+    cfg = O.Config(16, 24, 16, lx=0.5, ly=0.75, lz=0.5, nu=0.02, dt=1e-3, scheme=O.AB2_CN, bc=bc, pbc=pbc)
+    faces = random_faces(cfg, 21, amp=0.1)
+    cn_faces = [random_faces(cfg, 22 + d, amp=0.1) for d in range(3)]
+    st = random_state(cfg, 8, amp=0.2)
+    _run_compare(cfg, st, 5, faces=faces, cn_faces=cn_faces)
+
+
+def test_step_channel_graph_matches_eager():
+    cfg = O.Config(32, 16, 32, lx=2 * np.pi, ly=2.0, lz=np.pi, nu=1.0 / 180, dt=2e-3, scheme=O.AB2_CN,
+                   bc=(1, 2, 1), pbc=(1, 3, 1))
+    st = channel_state(cfg)
+    outs = []
+    for g in (0, 1):
+        with session(cfg, use_graph=g) as s:
+            s.set_state(st.u, st.v, st.w, st.p)
+            s.step(5)
+            outs.append(s.get_state())
+    for k in ("u", "v", "w", "p", "hx"):
+        assert np.array_equal(outs[0][k], outs[1][k])
+
+
+def test_unsupported_mixes_rejected():
+    from ns_3d_staggered_dp_gb300 import NSError
+    bad = [
+        dict(nx=32, ny=16, nz=32, bc=(2, 1, 1), pbc=(3, 1, 1)),   # wall x with periodic y/z
+        dict(nx=32, ny=256, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),  # dense y longer than 128
+        dict(nx=24, ny=16, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),   # FFT x not a power of two
+        dict(nx=25, ny=16, nz=32, bc=(2, 2, 2), pbc=(3, 3, 3)),   # odd wall x
+    ]
+    for kw in bad:
+        cfg = O.Config(kw["nx"], kw["ny"], kw["nz"], bc=kw["bc"], pbc=kw["pbc"])
+        with pytest.raises(NSError):
+            session(cfg)
