@@ -10,6 +10,13 @@ staggered u/v/w locations (synthetic; the reference's JHTDB-initialised
 256^3 state is not available).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload hit|channel]
+
+--workload channel measures the wall-bounded box instead: 256x128x256
+(x, z periodic; y no-slip walls with Neumann pressure), domain 2pi x 2 x 2pi,
+laminar profile u = 1 - (y-1)^2 plus a seeded divergence-free perturbation
+of amplitude 0.05, Re = 180, dt = 2e-3, AB2-CN with the mixed FFT-x/z and
+wall-y Poisson solve.
 
 metric: grid cell-steps per second (nx*ny*nz*steps / seconds), whole job.
 value : state resident in HBM, K steps replayed from a captured CUDA graph,
@@ -24,6 +31,7 @@ e2e   : the same metric through the C ABI with host buffers: every step
 from __future__ import annotations
 
 import argparse
+import functools
 import json
 import os
 import subprocess
@@ -51,6 +59,8 @@ ALG_DOUBLES = {
     "fft_x_inv": 2.0,     # read half spectrum, write dp
     "pr_bc": 0.0,         # ghost planes only
     "correct": 8.0,       # read u*, v*, w*, dp; write u, v, w, p
+    "fft_z_fwd": 2.0, "fft_z_inv": 2.0,        # wall-y box: z transforms of the half spectrum
+    "tri_y_solve": 2.0,   # read + write half spectrum (line solves along the wall axis)
 }
 
 # DRAM bytes per launch at 256^3 (dram__bytes_read.sum + dram__bytes_write.sum)
@@ -62,6 +72,7 @@ NCU_TRAFFIC_256 = {
 }
 
 
+@functools.lru_cache(maxsize=2)
 def hit_initial_field(n, k0=4.0, seed=2024):
     """Random-phase solenoidal field with E(k) ~ k^4 exp(-2 (k/k0)^2) on [0, 2pi]^3,
     unit rms velocity, sampled at the staggered locations, in the reference's
@@ -99,6 +110,51 @@ def hit_initial_field(n, k0=4.0, seed=2024):
     p = np.zeros((n + 2, n + 2, n + 2), order="F")
     umax = max(np.abs(comps[0]).max(), np.abs(comps[1]).max(), np.abs(comps[2]).max())
     return u, v, w, p, float(umax)
+
+
+def channel_initial_field(nx, ny, nz, ly=2.0, amp=0.05, seed=180):
+    """Laminar profile u = 1 - (y - 1)^2 between no-slip walls at y = 0, ly
+    plus a divergence-free perturbation: the discrete curl of a smooth seeded
+    vector potential (a_y, a_z) that vanishes on the walls, so the staggered
+    divergence is zero to rounding.  Reference padded shapes, ghosts filled
+    as vel_bc_staggered does with zero wall values."""
+    from oracle import ns_oracle as O
+    rng = np.random.default_rng(seed)
+    lx = lz = 2.0 * np.pi
+    dx, dy, dz = lx / nx, ly / ny, lz / nz
+    xf = dx * np.arange(nx + 1)             # x faces 1..nx+1
+    yf = dy * np.arange(ny + 1)
+    yc = dy * (np.arange(ny + 2) - 0.5)
+    zf = dz * np.arange(nz + 1)
+    zc = dz * (np.arange(nz + 2) - 0.5)
+    modes = [(rng.integers(1, 5), rng.integers(1, 5), rng.uniform(0, 2 * np.pi), rng.uniform(0, 2 * np.pi),
+              rng.standard_normal()) for _ in range(8)]
+
+    def pot(x, y, z, off):
+        env = (y * (ly - y)) ** 2
+        a = np.zeros((x.size, y.size, z.size))
+        for kx, kz, px, pz, c in modes:
+            a += c * (np.sin(kx * x + px + off)[:, None, None] * np.sin(kz * z + pz)[None, None, :])
+        return a * env[None, :, None]
+
+    # a_z on (x face, y face, z cell), a_y on (x face, y cell, z face):
+    # u = D_y a_z - D_z a_y, v = -D_x a_z, w = D_x a_y (exact discrete curl)
+    az = pot(xf, yf, zc, 0.0)
+    ay = pot(xf, yc, zf, 1.0)
+    u = np.zeros((nx + 1, ny + 2, nz + 2))
+    v = np.zeros((nx + 2, ny + 1, nz + 2))
+    w = np.zeros((nx + 2, ny + 2, nz + 1))
+    u[:, 1:ny + 1, :] = np.diff(az, axis=1) / dy
+    u[:, :, 1:nz + 1] -= np.diff(ay, axis=2) / dz
+    v[1:nx + 1] = -np.diff(az, axis=0) / dx
+    w[1:nx + 1] = np.diff(ay, axis=0) / dx
+    scale = amp / max(np.abs(u).max(), np.abs(v).max(), np.abs(w).max(), 1e-300)
+    u *= scale; v *= scale; w *= scale
+    u = u + (1.0 - (yc - 1.0) ** 2)[None, :, None]
+    u, v, w = np.asfortranarray(u), np.asfortranarray(v), np.asfortranarray(w)
+    O.vel_bc_staggered(u, v, w, O.Faces.zeros(nx, ny, nz), 1, 2, 1)
+    p = np.zeros((nx + 2, ny + 2, nz + 2), order="F")
+    return u, v, w, p
 
 
 class ClockSampler:
@@ -163,21 +219,50 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline_sample(n, steps, nu, dt):
-    """The oracle step (a NumPy/SciPy restatement of big_periodic_3D's loop body)
-    on the host cores, on `steps` steps of the n^3 workload."""
+def workload(name, n):
+    """Grid, initial state, step parameters and JSON config of a workload."""
+    if name == "channel":
+        nx, ny, nz = n, n // 2, n
+        nu, dt = 1.0 / 180.0, 2e-3
+        kw = dict(lx=2 * np.pi, ly=2.0, lz=2 * np.pi, nu=nu, dt=dt, scheme=2, bc=(1, 2, 1), pbc=(1, 3, 1))
+        cfgd = {"workload": f"{nx}x{ny}x{nz} wall-bounded box (x, z periodic; y no-slip walls, Neumann pressure), "
+                            "AB2-CN + FFT-x/z, line-solved y Poisson",
+                "grid": [nx, ny, nz], "domain": "2pi x 2 x 2pi", "scheme": "AB2-CN", "poisson": "FFT x/z + wall y",
+                "Re": 180, "nu": nu, "dt": dt, "seed": 180, "perturbation": 0.05, "dp_flag": 0,
+                "l2": f"inputs larger than L2 (state 7 x {(nx + 2) * (ny + 2) * (nz + 2) * 8 / 1e6:.0f} MB)"}
+        return dict(grid=(nx, ny, nz), kw=kw, config=cfgd,
+                    metric="FP64 grid cell-steps/s (256x128x256 wall-bounded box, AB2-CN + mixed FFT/wall Poisson)",
+                    init=lambda: channel_initial_field(nx, ny, nz))
+    nu = 1.0 / 1600.0
+    u, v, w, p, umax = hit_initial_field(n)
+    dt = 0.3 * (2 * np.pi / n) / umax
+    return dict(grid=(n, n, n), kw=dict(nu=nu, dt=dt, scheme=2), config=workload_config(n, dt), metric=METRIC,
+                init=lambda: (u, v, w, p))
+
+
+def oracle_setup(name, n):
     from oracle import ns_oracle as O
-    u, v, w, p, _ = hit_initial_field(n)
-    cfg = O.Config(n, n, n, nu=nu, dt=dt, scheme=O.AB2_CN)
+    W = workload(name, n)
+    nx, ny, nz = W["grid"]
+    kw = dict(W["kw"])
+    cfg = O.Config(nx, ny, nz, **kw)
+    u, v, w, p = W["init"]()
     st = O.State(u, v, w, p, np.zeros_like(u), np.zeros_like(v), np.zeros_like(w), first=True)
-    dx = cfg.h[0]
-    cnf = O.CNFactors(n, n, n, cfg.bc, dx * dx, dx * dx, dx * dx, dt, nu)
+    dx, dy, dz = cfg.h
+    cnf = O.CNFactors(nx, ny, nz, cfg.bc, dx * dx, dy * dy, dz * dz, cfg.dt, cfg.nu)
+    return O, cfg, st, cnf, nx * ny * nz
+
+
+def cpu_baseline_sample(name, n, steps):
+    """The oracle step (a NumPy/SciPy restatement of the reference loop body)
+    on the host cores, on `steps` steps of the workload at grid size n."""
+    O, cfg, st, cnf, ncell = oracle_setup(name, n)
     st = O.step(st, cfg, cnf=cnf)  # warm (Euler start)
     t0 = time.perf_counter()
     for _ in range(steps):
         st = O.step(st, cfg, cnf=cnf)
     sec = time.perf_counter() - t0
-    return n ** 3 * steps / sec, sec
+    return ncell * steps / sec, sec
 
 
 def run_reference(args):
@@ -185,15 +270,9 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from oracle import ns_oracle as O
     n = args.n
-    u, v, w, p, umax = hit_initial_field(n)
-    nu = 1.0 / 1600.0
-    dt = 0.3 * (2 * np.pi / n) / umax
-    cfg = O.Config(n, n, n, nu=nu, dt=dt, scheme=O.AB2_CN)
-    st = O.State(u, v, w, p, np.zeros_like(u), np.zeros_like(v), np.zeros_like(w), first=True)
-    dx = cfg.h[0]
-    cnf = O.CNFactors(n, n, n, cfg.bc, dx * dx, dx * dx, dx * dx, dt, nu)
+    W = workload(args.workload, n)
+    O, cfg, st, cnf, ncell = oracle_setup(args.workload, n)
     for _ in range(max(1, min(args.warmup, 1))):
         st = O.step(st, cfg, cnf=cnf)  # untimed (includes the Euler start)
     per_step = []
@@ -204,14 +283,14 @@ def run_reference(args):
         if sum(per_step) > args.ref_budget_s:
             break
     sec = float(np.median(per_step))
-    value = n ** 3 / sec
+    value = ncell / sec
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "impl": "reference", "metric": W["metric"], "value": value, "unit": UNIT, "n_gpus": world,
         "steps": len(per_step), "warmup": 1, "ms_per_step": 1e3 * sec,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": workload_config(n, dt),
+        "data": "synthetic", "config": W["config"],
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{len(per_step)} step(s) of the {n}^3 AB2-CN workload after one untimed "
+                         "sample": f"{len(per_step)} step(s) of the full workload after one untimed "
                                    "Euler-start step; NumPy/SciPy restatement of the reference step "
                                    "(the Fortran/MKL reference cannot be built here), threaded BLAS"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -238,11 +317,11 @@ def run_ours(args):
     from ns_3d_staggered_dp_gb300 import Session, make_config
 
     n = args.n
-    u, v, w, p, umax = hit_initial_field(n)
-    nu = 1.0 / 1600.0
-    dt = 0.3 * (2 * np.pi / n) / umax
-    cfg = make_config(n, n, n, nu=nu, dt=dt, scheme=2)
-    ncell = n ** 3
+    W = workload(args.workload, n)
+    nx, ny, nz = W["grid"]
+    u, v, w, p = W["init"]()
+    cfg = make_config(nx, ny, nz, **W["kw"])
+    ncell = nx * ny * nz
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     with Session(cfg) as s:
@@ -330,14 +409,15 @@ def run_ours(args):
     per_launch_ms = dms / max(1, dl)
     alg_bytes = ALG_DOUBLES.get(dname, 0.0) * 8.0 * ncell
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
-    traffic = NCU_TRAFFIC_256.get(dname) if n == 256 else None
+    traffic = NCU_TRAFFIC_256.get(dname) if (n == 256 and args.workload == "hit") else None
     total_prof = sum(v[0] for v in prof.values())
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": W["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded k^4 exp(-2(k/4)^2) solenoidal field, unit rms; no dataset)",
-        "config": workload_config(n, dt) | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "data": ("synthetic (seeded k^4 exp(-2(k/4)^2) solenoidal field, unit rms; no dataset)"
+                 if args.workload == "hit" else "synthetic (laminar profile + seeded divergence-free perturbation)"),
+        "config": W["config"] | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "steps": e2e_steps, "path": "ns_set_state (pinned host) + ns_step + ns_get_state (pinned host)"},
         "gpu_launches": launches,
@@ -352,9 +432,11 @@ def run_ours(args):
     }
     if args.cpu_baseline:
         try:
-            cv, csec = cpu_baseline_sample(min(n, args.cpu_n), 1, nu, dt)
+            cn = min(n, args.cpu_n)
+            cv, csec = cpu_baseline_sample(args.workload, cn, 1)
+            g = workload(args.workload, cn)["grid"]
             line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                                    "sample": f"1 step of the {min(n, args.cpu_n)}^3 AB2-CN workload "
+                                    "sample": f"1 step of the workload at {g[0]}x{g[1]}x{g[2]} "
                                               f"({csec:.1f} s), NumPy/SciPy oracle restatement, threaded BLAS/FFT"}
         except Exception as e:  # the baseline never blocks the GPU line
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -366,7 +448,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
@@ -374,6 +456,7 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--ref-budget-s", type=float, default=60.0)
+    ap.add_argument("--workload", default="hit", choices=["hit", "channel"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

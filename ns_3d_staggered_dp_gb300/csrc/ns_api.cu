@@ -258,10 +258,18 @@ int validate(const ns_config& c, std::string& msg) {
   }
   auto pow2 = [](int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512; };
   const int n3[3] = {c.nx, c.ny, c.nz};
+  // Wall axes: a wall z (else a wall y) is solved line by line (tridiagonal),
+  // a wall y in front of a wall z and a wall x are dense transforms.
+  const int sax = c.pbc[2] != 1 ? 2 : (c.pbc[1] != 1 ? 1 : 0);
   for (int a = 0; a < 3; ++a) {
     if (c.pbc[a] == 1 && !pow2(n3[a])) { msg = "FFT (periodic) axes must be powers of two in [16, 512]"; return NS_ERR_SHAPE; }
-    if (c.pbc[a] != 1 && a > 0 && n3[a] > 128) { msg = "non-periodic y/z axes are limited to 128 cells"; return NS_ERR_SHAPE; }
-    if (c.pbc[a] != 1 && a == 0 && (n3[a] % 2 != 0 || n3[a] > 1024)) {
+    if (c.pbc[a] == 1) continue;
+    if (a == sax && n3[a] > (c.pbc[0] != 1 ? 256 : 512)) {
+      msg = "the wall axis solved by lines is limited to 512 cells (256 with a wall x)";
+      return NS_ERR_SHAPE;
+    }
+    if (a == 1 && a != sax && n3[a] > 128) { msg = "a wall y in front of a wall z is limited to 128 cells"; return NS_ERR_SHAPE; }
+    if (a == 0 && (n3[a] % 2 != 0 || n3[a] > 1024)) {
       msg = "a non-periodic x axis needs an even cell count <= 1024";
       return NS_ERR_SHAPE;
     }
@@ -447,7 +455,13 @@ int build_plans(ns_handle* h) {
   const double hs[3] = {h->dx, h->dy, h->dz};
   FftPlan& P = h->plan;
   P = FftPlan{};
+  // Axis roles: FFT on periodic axes; a wall z (else a wall y) is the
+  // tridiagonal solve axis; the other wall axes get dense transforms.
   for (int a = 0; a < 3; ++a) P.kind[a] = c.pbc[a] == 1 ? 0 : 1;
+  int sax = 0;  // solve axis (0: the fused FFT z solve)
+  if (P.kind[2] == 1) sax = 2;
+  else if (P.kind[1] == 1) sax = 1;
+  if (sax) P.kind[sax] = 2;
   const bool xper = P.kind[0] == 0;
   const int nxs = xper ? nxh : nx / 2;
   // Twiddles W_N^m = exp(-2 pi i m / N), computed in long double (FFT axes only).
@@ -472,11 +486,32 @@ int build_plans(ns_handle* h) {
   if (tw.empty()) tw.push_back(make_double2(1.0, 0.0));
   NS_CUDA(h, cudaMalloc(&h->tw, tw.size() * sizeof(double2)));
   NS_CUDA(h, cudaMemcpyAsync(h->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
-  // Dense transform matrices: x stored transposed (F^T, G^T), y and z as is.
-  std::vector<double> dense;
-  size_t o_f[3] = {0, 0, 0}, o_g[3] = {0, 0, 0};
+  // Per-axis eigenvalues lambda = -4 sin^2(..)/h^2 of each mode.
+  std::vector<double> e3[3];
   for (int a = 0; a < 3; ++a) {
-    if (P.kind[a] == 0) continue;
+    const int cnt = (a == 0 && xper) ? nxh : n3[a];
+    e3[a].resize(cnt);
+    for (int m = 0; m < cnt; ++m) e3[a][m] = -4.0 * axis_eig(n3[a], c.pbc[a], m, hs[a]);
+  }
+  // Scale of the unnormalised FFT passes (x: 2 nx for the r2c/c2r pair); the
+  // dense pairs are exact inverses.
+  double scale = 1.0;
+  if (xper) scale /= 2.0 * nx;
+  if (P.kind[1] == 0) scale /= ny;
+  if (P.kind[2] == 0) scale /= nz;
+  const bool allper = c.pbc[0] == 1 && c.pbc[1] == 1 && c.pbc[2] == 1;
+  bool singular = true;
+  for (int a = 0; a < 3; ++a) singular = singular && (c.pbc[a] == 1 || c.pbc[a] == 3);
+  // The singular mode: zero mean for the all-periodic FFT solve
+  // (big_periodic_3D.f90:242-255), mean_dp otherwise (NS_functions.f90:1576-1577).
+  P.has_mean = (singular && !allper) ? 1 : 0;
+  // Device tables: dense matrices (x stored transposed: F^T, G^T), then the
+  // eigenvalue tables of the tridiagonal solve, or the 1/lambda table of the
+  // FFT z solve.
+  std::vector<double> tab;
+  size_t o_f[3] = {0, 0, 0}, o_g[3] = {0, 0, 0}, o_ex = 0, o_eo = 0, o_il = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (P.kind[a] != 1) continue;
     std::vector<double> F, G;
     dense_pair(n3[a], c.pbc[a], F, G);
     const int n = n3[a];
@@ -490,72 +525,54 @@ int build_plans(ns_handle* h) {
       F.swap(Ft);
       G.swap(Gt);
     }
-    o_f[a] = dense.size();
-    dense.insert(dense.end(), F.begin(), F.end());
-    o_g[a] = dense.size();
-    dense.insert(dense.end(), G.begin(), G.end());
+    o_f[a] = tab.size();
+    tab.insert(tab.end(), F.begin(), F.end());
+    o_g[a] = tab.size();
+    tab.insert(tab.end(), G.begin(), G.end());
   }
-  // Eigenvalues lambda = -4 (ex + ey + ez), inverted with the pipeline's
-  // scale: each FFT pass is unnormalised (x: 2 nx for the r2c/c2r pair), the
-  // dense pairs are exact inverses.
-  std::vector<double> e3[3];
-  for (int a = 0; a < 3; ++a) {
-    const int cnt = (a == 0 && xper) ? nxh : n3[a];
-    e3[a].resize(cnt);
-    for (int m = 0; m < cnt; ++m) e3[a][m] = axis_eig(n3[a], c.pbc[a], m, hs[a]);
-  }
-  double scale = 1.0;
-  if (xper) scale /= 2.0 * nx;
-  if (P.kind[1] == 0) scale /= ny;
-  if (P.kind[2] == 0) scale /= nz;
-  const bool allper = c.pbc[0] == 1 && c.pbc[1] == 1 && c.pbc[2] == 1;
-  bool singular = true;
-  for (int a = 0; a < 3; ++a) singular = singular && (c.pbc[a] == 1 || c.pbc[a] == 3);
-  // The singular mode: zero mean for the all-periodic FFT solve
-  // (big_periodic_3D.f90:242-255), mean_dp otherwise (NS_functions.f90:1576-1577).
-  P.has_mean = (singular && !allper) ? 1 : 0;
-  double dense_prod = 1.0;
-  for (int a = 0; a < 3; ++a)
-    if (P.kind[a] == 1) dense_prod *= n3[a];
-  P.mean_val = c.mean_dp * dense_prod;
   const size_t nspec = (size_t)nxs * ny * nz;
-  auto inv_of = [&](int i, int j, int k) {
-    if (i == 0 && j == 0 && k == 0 && singular) return 0.0;
-    const double lam = -4.0 * ((e3[0][i] + e3[1][j]) + e3[2][k]);
-    return scale / lam;
-  };
-  std::vector<double> il;
-  std::vector<double2> il2;
-  if (P.kind[2] == 0) il.resize(nspec);
-  else il2.resize(nspec);
-  for (int k = 0; k < nz; ++k)
-    for (int j = 0; j < ny; ++j)
-      for (int i = 0; i < nxs; ++i) {
-        const size_t g = i + (size_t)nxs * (j + (size_t)ny * k);
-        if (P.kind[2] == 0) il[g] = inv_of(i, j, k);
-        else if (xper) il2[g] = make_double2(inv_of(i, j, k), inv_of(i, j, k));
-        else il2[g] = make_double2(inv_of(2 * i, j, k), inv_of(2 * i + 1, j, k));
-      }
-  // One buffer: 1/lambda table (double or double2), then the dense matrices.
-  const size_t n_il = il.empty() ? 2 * il2.size() : il.size();
-  const size_t n_dense = dense.size();
-  NS_CUDA(h, cudaMalloc(&h->inv_lam, (n_il + n_dense + 1) * sizeof(double)));
-  if (!il.empty())
-    NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, il.data(), il.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  else
-    NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, il2.data(), il2.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
-  double* dbase = h->inv_lam + n_il;
-  if (n_dense)
-    NS_CUDA(h, cudaMemcpyAsync(dbase, dense.data(), n_dense * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if (sax) {
+    const int oax = 3 - sax;
+    o_ex = tab.size();
+    tab.insert(tab.end(), e3[0].begin(), e3[0].end());
+    o_eo = tab.size();
+    tab.insert(tab.end(), e3[oax].begin(), e3[oax].end());
+    const double hh = hs[sax];
+    const int pb = c.pbc[sax];
+    const double e_end = pb == 2 ? -1.0 : (pb == 3 ? 1.0 : 0.0);
+    P.tri_h2 = hh * hh;
+    P.tri_rs = hh * hh * scale;
+    P.tri_elo = P.tri_ehi = e_end;
+    double dense_other = 1.0;
+    for (int a = 0; a < 3; ++a)
+      if (a != sax && P.kind[a] == 1) dense_other *= n3[a];
+    P.mean_val = c.mean_dp * dense_other;  // mean of the singular line
+  } else {
+    o_il = tab.size();
+    tab.resize(tab.size() + nspec);
+    double* il = tab.data() + o_il;
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nxh; ++i) {
+          const double lam = (e3[0][i] + e3[1][j]) + e3[2][k];
+          il[i + (size_t)nxh * (j + (size_t)ny * k)] = (i == 0 && j == 0 && k == 0) ? 0.0 : scale / lam;
+        }
+    P.mean_val = 0.0;
+  }
+  if (tab.empty()) tab.push_back(0.0);
+  NS_CUDA(h, cudaMalloc(&h->inv_lam, tab.size() * sizeof(double)));
+  NS_CUDA(h, cudaMemcpyAsync(h->inv_lam, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
   NS_CUDA(h, cudaMalloc(&h->spec, nspec * sizeof(double2)));
+  const double* t0 = h->inv_lam;
   P.nx = nx; P.ny = ny; P.nz = nz; P.nxh = nxh; P.nxs = nxs;
   P.tw_x = h->tw; P.tw_xr = h->tw + o_xr; P.tw_y = h->tw + o_y; P.tw_z = h->tw + o_z;
-  P.inv_lam = il.empty() ? nullptr : h->inv_lam;
-  P.inv_lam2 = il.empty() ? reinterpret_cast<const double2*>(h->inv_lam) : nullptr;
+  P.inv_lam = sax ? nullptr : t0 + o_il;
+  P.eig_x = sax ? t0 + o_ex : nullptr;
+  P.eig_o = sax ? t0 + o_eo : nullptr;
   for (int a = 0; a < 3; ++a) {
-    P.fwd[a] = P.kind[a] ? dbase + o_f[a] : nullptr;
-    P.inv[a] = P.kind[a] ? dbase + o_g[a] : nullptr;
+    P.fwd[a] = P.kind[a] == 1 ? t0 + o_f[a] : nullptr;
+    P.inv[a] = P.kind[a] == 1 ? t0 + o_g[a] : nullptr;
   }
   // pr_bc_staggered_modify_rhs coefficients (NS_functions.f90:1345-1400) and
   // the set-0 pressure face planes they read.

@@ -16,8 +16,11 @@
 // y/z passes act on the complex half spectrum (real and imaginary parts
 // transform alike).  With every axis non-periodic the x pass applies F_x to
 // the real divergence line and packs modes (2q, 2q+1) into one complex value,
-// so the y/z passes again act on complex lines; the solve scales the real and
-// imaginary parts by their own eigenvalues (double2 table).
+// so the y/z passes again act on complex lines.  The wall axis that is
+// transformed last is not transformed at all: its lines are solved as
+// tridiagonal systems (tri_solve_kernel), which gives the same solution as
+// transform, eigenvalue divide and inverse transform along that axis; with
+// packed x modes the real and imaginary parts are two systems.
 // The divergence kernels add the pressure-BC terms of
 // pr_bc_staggered_modify_rhs (NS_functions.f90:1345-1400) on the first and
 // last cells of every non-periodic axis.
@@ -100,9 +103,8 @@ __global__ void __launch_bounds__(128) dense_x_inv_kernel(SpecPlan S, const doub
 }
 
 // Dense transform of complex lines along y (AXIS 1) or z (AXIS 2), lanes over
-// consecutive spectrum columns (coalesced).  With SOLVE (z only): forward,
-// scale by the eigenvalue table, inverse, all on chip.
-template <int AXIS, bool FWD, bool SOLVE>
+// consecutive spectrum columns (coalesced).
+template <int AXIS, bool FWD>
 __global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __restrict__ spec) {
   extern __shared__ __align__(16) double2 ls[];
   constexpr int LPC = 16, T = 8;  // 16 lines (columns) x 8 threads per line
@@ -118,7 +120,7 @@ __global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __re
   if (valid)
     for (int n = t; n < N; n += T) line[n * LPC] = g[(long long)n * st];
   __syncthreads();
-  const double* __restrict__ M = (SOLVE || FWD) ? S.fwd[AXIS] : S.inv[AXIS];
+  const double* __restrict__ M = FWD ? S.fwd[AXIS] : S.inv[AXIS];
   // outputs k = t + T*q
   double2 acc[16];
   const int nq = (N + T - 1) / T;
@@ -138,49 +140,124 @@ __global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __re
       }
     }
   }
-  if (SOLVE) {
-    // scale by 1/lambda per (real, imaginary) part; the singular mode takes the mean value
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int kk = t + T * q;
-      if (q < nq && kk < N && valid) {
-        const long long gi = base + (long long)kk * st;
-        const double2 s = __ldg(S.inv_lam2 + gi);
-        acc[q].x *= s.x;
-        acc[q].y *= s.y;
-        if (S.has_mean && gi == 0) acc[q].x = S.mean_val;
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int kk = t + T * q;
-      if (q < nq && kk < N) line[kk * LPC] = acc[q];
-    }
-    __syncthreads();
-    const double* __restrict__ Gm = S.inv[AXIS];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] = make_double2(0.0, 0.0);
-    for (int n = 0; n < N; ++n) {
-      const double2 v = line[n * LPC];
-#pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        if (q < nq) {
-          const int kk = t + T * q;
-          if (kk < N) {
-            const double m = __ldg(Gm + (long long)kk * N + n);
-            acc[q].x = fma(m, v.x, acc[q].x);
-            acc[q].y = fma(m, v.y, acc[q].y);
-          }
-        }
-      }
-    }
-  }
   if (!valid) return;
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int kk = t + T * q;
     if (q < nq && kk < N) g[(long long)kk * st] = acc[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tridiagonal solve along the wall axis s.  After the transforms of the other
+// two axes every spectrum line along s is an independent system
+//   p[j-1] - (2 - e_j - sigma h^2) p[j] + p[j+1] = h^2 scale rhs[j],
+// sigma = lambda_x + lambda_other, e_j the pressure-BC change of the end rows.
+// Its solution is that of the per-axis transform, eigenvalue divide and
+// inverse transform of DCT_poisson_solver (NS_functions.f90:1505-1630) along s.
+// One thread per line (Thomas, no pivoting: the rows are diagonally
+// dominant); the multipliers go to shared memory, the forward-eliminated rhs
+// back to the line in place.  The one singular line (Neumann/periodic
+// everywhere, both modes 0) drops its rhs mean, pins its last entry and takes
+// the mean value (NS_functions.f90:1576-1577).
+// ---------------------------------------------------------------------------
+constexpr int TRI_T = 32;  // lines per CTA (one warp)
+
+// One real component of a line, general path (the singular line).
+__device__ void tri_real(double* x, long long sx, int N, double sig_h2, double elo, double ehi, double rs, double* cm,
+                         bool sing, double target) {
+  double mean_r = 0.0;
+  if (sing) {
+    for (int j = 0; j < N; ++j) mean_r += x[j * sx];
+    mean_r /= N;
+  }
+  const int last = sing ? N - 2 : N - 1;
+  double m = 0.0, d = 0.0;
+  for (int j = 0; j <= last; ++j) {
+    double b = -2.0 + sig_h2;
+    if (j == 0) b += elo;
+    if (j == N - 1) b += ehi;
+    m = 1.0 / (b - m);
+    d = fma(x[j * sx] - mean_r, rs, -d) * m;
+    x[j * sx] = d;
+    cm[j * TRI_T] = m;
+  }
+  double p = 0.0;
+  if (sing) x[(long long)(N - 1) * sx] = 0.0;
+  else p = d;
+  for (int j = N - 2; j >= 0; --j) {
+    p = fma(-cm[j * TRI_T], p, x[j * sx]);
+    x[j * sx] = p;
+  }
+  if (sing) {
+    double mp = 0.0;
+    for (int j = 0; j < N; ++j) mp += x[j * sx];
+    const double shift = target - mp / N;
+    for (int j = 0; j < N; ++j) x[j * sx] += shift;
+  }
+}
+
+template <int AXIS, bool PACKED>
+__global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* __restrict__ spec) {
+  extern __shared__ __align__(16) double cm[];  // [N][TRI_T] multipliers (x2 when PACKED)
+  const int l = threadIdx.x;
+  const int N = AXIS == 1 ? S.ny : S.nz;
+  const int n_other = AXIS == 1 ? S.nz : S.ny;
+  // Columns: with a periodic x the Nyquist column is handled by the last
+  // block column, lanes over the other index (no idle lanes).
+  const int nreg = PACKED ? S.nxs : S.nxs - 1;
+  const int nblk = (nreg + TRI_T - 1) / TRI_T;
+  int col, o;
+  bool valid;
+  if ((int)blockIdx.x < nblk) {
+    col = blockIdx.x * TRI_T + l;
+    o = blockIdx.y;
+    valid = col < nreg;
+  } else {
+    if ((int)blockIdx.y * TRI_T >= n_other) return;
+    col = S.nxs - 1;
+    o = blockIdx.y * TRI_T + l;
+    valid = o < n_other;
+  }
+  if (!valid) return;
+  const long long st = AXIS == 1 ? (long long)S.nxs : (long long)S.nxs * S.ny;
+  double2* g = spec + (AXIS == 1 ? col + (long long)S.nxs * S.ny * o : col + (long long)S.nxs * o);
+  const double lo = __ldg(S.eig_o + o);
+  const double sr = (__ldg(S.eig_x + (PACKED ? 2 * col : col)) + lo) * S.tri_h2;
+  const double si = PACKED ? (__ldg(S.eig_x + 2 * col + 1) + lo) * S.tri_h2 : sr;
+  const double rs = S.tri_rs, elo = S.tri_elo, ehi = S.tri_ehi;
+  double* cmr = cm + l;
+  double* cmi = PACKED ? cm + (long long)N * TRI_T + l : cmr;
+  if (S.has_mean && col == 0 && o == 0) {  // the singular line
+    double* x = reinterpret_cast<double*>(g);
+    tri_real(x, 2 * st, N, sr, elo, ehi, rs, cmr, true, S.mean_val);
+    tri_real(x + 1, 2 * st, N, si, elo, ehi, rs, cmi, !PACKED, 0.0);
+    return;
+  }
+  double mr = 0.0, mi = 0.0;
+  double2 d = make_double2(0.0, 0.0);
+#pragma unroll 4
+  for (int j = 0; j < N; ++j) {
+    double br = -2.0 + sr, bi = -2.0 + si;
+    if (j == 0) { br += elo; bi += elo; }
+    if (j == N - 1) { br += ehi; bi += ehi; }
+    mr = 1.0 / (br - mr);
+    if (PACKED) mi = 1.0 / (bi - mi);
+    else mi = mr;
+    const double2 r = g[(long long)j * st];
+    d.x = fma(r.x, rs, -d.x) * mr;
+    d.y = fma(r.y, rs, -d.y) * mi;
+    g[(long long)j * st] = d;
+    cmr[j * TRI_T] = mr;
+    if (PACKED) cmi[j * TRI_T] = mi;
+  }
+  double2 p = d;
+#pragma unroll 4
+  for (int j = N - 2; j >= 0; --j) {
+    const double2 x = g[(long long)j * st];
+    p.x = fma(-cmr[j * TRI_T], p.x, x.x);
+    p.y = fma(-cmi[j * TRI_T], p.y, x.y);
+    g[(long long)j * st] = p;
   }
 }
 
@@ -193,15 +270,32 @@ cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double
   return cudaGetLastError();
 }
 
-cudaError_t launch_dense_yz(int axis, int mode, const SpecPlan& S, double2* spec, cudaStream_t st) {
+cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st) {
   const int N = axis == 1 ? S.ny : S.nz;
   if (N > 128) return cudaErrorInvalidValue;
   const size_t sm = (size_t)N * 16 * sizeof(double2);
   dim3 grid((S.nxs + 15) / 16, axis == 1 ? S.nz : S.ny);
-  if (axis == 1 && mode == 0) dense_yz_kernel<1, true, false><<<grid, 128, sm, st>>>(S, spec);
-  else if (axis == 1 && mode == 1) dense_yz_kernel<1, false, false><<<grid, 128, sm, st>>>(S, spec);
-  else if (axis == 2 && mode == 2) dense_yz_kernel<2, true, true><<<grid, 128, sm, st>>>(S, spec);
-  else return cudaErrorInvalidValue;
+  if (axis == 1 && fwd) dense_yz_kernel<1, true><<<grid, 128, sm, st>>>(S, spec);
+  else if (axis == 1) dense_yz_kernel<1, false><<<grid, 128, sm, st>>>(S, spec);
+  else if (fwd) dense_yz_kernel<2, true><<<grid, 128, sm, st>>>(S, spec);
+  else dense_yz_kernel<2, false><<<grid, 128, sm, st>>>(S, spec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st) {
+  const int N = axis == 1 ? S.ny : S.nz;
+  const int n_other = axis == 1 ? S.nz : S.ny;
+  const bool packed = S.kind[0] != 0;
+  const size_t sm = (size_t)N * TRI_T * sizeof(double) * (packed ? 2 : 1);
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  const int nreg = packed ? S.nxs : S.nxs - 1;
+  const int nblk = (nreg + TRI_T - 1) / TRI_T;
+  dim3 grid(nblk + (packed ? 0 : 1), n_other);
+  auto kern = axis == 1 ? (packed ? tri_solve_kernel<1, true> : tri_solve_kernel<1, false>)
+                        : (packed ? tri_solve_kernel<2, true> : tri_solve_kernel<2, false>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, TRI_T, sm, st>>>(S, spec);
   return cudaGetLastError();
 }
 

@@ -254,19 +254,22 @@ __device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, in
   return G;
 }
 
-template <int N, int DIR>
-__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_y_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+// Complex FFT along y (AXIS 1) or z (AXIS 2), forward (DIR -1) or inverse.
+template <int AXIS, int N, int DIR>
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_yz_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
   using F = YZ<N>;
   constexpr int LPC = F::LPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* sb = reinterpret_cast<double2*>(smem_raw);
   const int l = threadIdx.x, t = threadIdx.y;
-  const LineGeo G = yz_line(1, P.nxh, P.ny, P.nz, l, LPC);
-  if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && blockIdx.y * LPC >= (unsigned)P.nz) return;  // whole block idle
+  const LineGeo G = yz_line(AXIS, P.nxh, P.ny, P.nz, l, LPC);
+  const int n_other = AXIS == 1 ? P.nz : P.ny;
+  if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && blockIdx.y * LPC >= (unsigned)n_other) return;  // whole block idle
   double2* g = spec + G.base;
-  const long long st = P.nxh;
+  const long long st = AXIS == 1 ? (long long)P.nxh : (long long)P.nxh * P.ny;
+  const double2* tw = AXIS == 1 ? P.tw_y : P.tw_z;
   if (DIR < 0) {
-    if (G.valid) F::fwdA(g, st, sb, P.tw_y, l, t, c);
+    if (G.valid) F::fwdA(g, st, sb, tw, l, t, c);
     __syncthreads();
     double2 xk[F::KQ][F::R1];
     F::fwdB(xk, sb, l, t, c);
@@ -283,7 +286,7 @@ __global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_y_kernel(FftPlan 
 #pragma unroll
       for (int k1 = 0; k1 < F::R1; ++k1)
         xk[q][k1] = G.valid ? g[(long long)(t + F::T * q + F::R2 * k1) * st] : make_double2(0.0, 0.0);
-    F::invA(xk, sb, P.tw_y, l, t, c);
+    F::invA(xk, sb, tw, l, t, c);
     __syncthreads();
     if (G.valid) F::invB(g, st, sb, l, t, c);
   }
@@ -529,15 +532,16 @@ cudaError_t launch_x_inv(const FftPlan& P, const double2* spec, double* dp, cons
   kern<<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, spec, dp, L, c);
   return cudaGetLastError();
 }
-template <int N, int DIR>
-cudaError_t launch_y(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
+template <int AXIS, int N, int DIR>
+cudaError_t launch_yz(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
   const size_t sm = yz_smem<N>();
-  cudaError_t e = cudaFuncSetAttribute(fft_y_kernel<N, DIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  auto kern = fft_yz_kernel<AXIS, N, DIR>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   constexpr int LPC = lpc<N>();
-  dim3 grid(yz_nblk(P.nxh, LPC) + 1, P.nz);
+  dim3 grid(yz_nblk(P.nxh, LPC) + 1, AXIS == 1 ? P.nz : P.ny);
   dim3 block(LPC, Split<N>::R1);
-  fft_y_kernel<N, DIR><<<grid, block, sm, st>>>(P, spec, c);
+  kern<<<grid, block, sm, st>>>(P, spec, c);
   return cudaGetLastError();
 }
 template <int N>
@@ -585,35 +589,51 @@ cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec
     if ((e = launch_dense_x(true, P, d, spec, dp, L, st)) != cudaSuccess) return e;
     mk("dense_x_fwd");
   }
-  if (P.kind[1] == 0) {
-#define Y_FWD(n) e = launch_y<(n), -1>(P, spec, c, st)
-    NS_SIZE_SWITCH(P.ny, Y_FWD)
+  // The middle axis m is transformed, the solve axis s is solved per line:
+  // (m, s) = (y, z) unless y is the wall axis of a z-periodic box.
+  const int m = P.kind[1] == 2 ? 2 : 1;
+  const int nm = m == 1 ? P.ny : P.nz;
+  if (P.kind[m] == 0) {
+    if (m == 1) {
+#define Y_FWD(n) e = launch_yz<1, (n), -1>(P, spec, c, st)
+      NS_SIZE_SWITCH(nm, Y_FWD)
 #undef Y_FWD
+    } else {
+#define Z_FWD(n) e = launch_yz<2, (n), -1>(P, spec, c, st)
+      NS_SIZE_SWITCH(nm, Z_FWD)
+#undef Z_FWD
+    }
     if (e != cudaSuccess) return e;
-    mk("fft_y_fwd");
+    mk(m == 1 ? "fft_y_fwd" : "fft_z_fwd");
   } else {
-    if ((e = launch_dense_yz(1, 0, P, spec, st)) != cudaSuccess) return e;
-    mk("dense_y_fwd");
+    if ((e = launch_dense_yz(m, true, P, spec, st)) != cudaSuccess) return e;
+    mk(m == 1 ? "dense_y_fwd" : "dense_z_fwd");
   }
-  if (P.kind[2] == 0) {
+  if (P.kind[2] == 0 && P.kind[1] != 2) {
 #define Z_SOL(n) e = launch_z<(n)>(P, spec, c, st)
     NS_SIZE_SWITCH(P.nz, Z_SOL)
 #undef Z_SOL
     if (e != cudaSuccess) return e;
     mk("fft_z_solve");
   } else {
-    if ((e = launch_dense_yz(2, 2, P, spec, st)) != cudaSuccess) return e;
-    mk("dense_z_solve");
+    if ((e = launch_tri_solve(3 - m, P, spec, st)) != cudaSuccess) return e;
+    mk(m == 1 ? "tri_z_solve" : "tri_y_solve");
   }
-  if (P.kind[1] == 0) {
-#define Y_INV(n) e = launch_y<(n), 1>(P, spec, c, st)
-    NS_SIZE_SWITCH(P.ny, Y_INV)
+  if (P.kind[m] == 0) {
+    if (m == 1) {
+#define Y_INV(n) e = launch_yz<1, (n), 1>(P, spec, c, st)
+      NS_SIZE_SWITCH(nm, Y_INV)
 #undef Y_INV
+    } else {
+#define Z_INV(n) e = launch_yz<2, (n), 1>(P, spec, c, st)
+      NS_SIZE_SWITCH(nm, Z_INV)
+#undef Z_INV
+    }
     if (e != cudaSuccess) return e;
-    mk("fft_y_inv");
+    mk(m == 1 ? "fft_y_inv" : "fft_z_inv");
   } else {
-    if ((e = launch_dense_yz(1, 1, P, spec, st)) != cudaSuccess) return e;
-    mk("dense_y_inv");
+    if ((e = launch_dense_yz(m, false, P, spec, st)) != cudaSuccess) return e;
+    mk(m == 1 ? "dense_y_inv" : "dense_z_inv");
   }
   if (P.kind[0] == 0) {
 #define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st)

@@ -137,12 +137,18 @@ struct FftPlan {
   const double* inv_lam;  // scale/lambda per spectrum entry (FFT z solve), 0 at the mean mode
   int dp_unaligned;       // 1: dp slot pairs (2m+1, 2m+2) are not 16-byte aligned (scalar stores)
   int nxs;                // spectrum row length: nx/2+1 (periodic x) or nx/2 (packed wall x)
-  int kind[3];            // 0: FFT axis, 1: dense transform axis
+  int kind[3];            // 0: FFT axis, 1: dense transform axis, 2: tridiagonal solve axis (a wall)
   const double* fwd[3];   // dense forward matrices (x: F^T [n][k]; y, z: F [k][n])
   const double* inv[3];   // dense inverse matrices (x: G^T [k][n]; y, z: G [n][k])
-  const double2* inv_lam2;  // (re, im) scales of the dense z solve
   int has_mean;           // 1: the singular mode is set to mean_val (after the forward passes)
-  double mean_val;
+  double mean_val;        // FFT z solve: the singular entry; tridiagonal solve: the singular line's mean
+  // Tridiagonal solve along the wall axis s, one line per (x mode, other-axis mode):
+  // rows (p[j-1] - (2 - e_j - sigma h^2) p[j] + p[j+1]) = h^2 scale rhs[j].
+  const double* eig_x;    // lambda of the x modes (nxs entries; 2 per entry when x is packed)
+  const double* eig_o;    // lambda of the modes of the remaining axis
+  double tri_h2;          // h_s^2
+  double tri_rs;          // h_s^2 * scale of the unnormalised FFT passes
+  double tri_elo, tri_ehi;  // end-row diagonal changes: pbc 2 -1, pbc 3 +1, pbc 4 0
   double mod_lo[3], mod_hi[3];        // pr_bc_staggered_modify_rhs coefficients per axis
   const double* face_lo[3];           // pressure face planes per axis (internal slot order)
   const double* face_hi[3];
@@ -182,10 +188,12 @@ struct DivArgs {
 // The spectral solve (FFT and dense axes mixed), divergence to dp interior.
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk);
-// Dense passes (ns_dct.cu): x forward/inverse; y/z mode 0 forward, 1 inverse, 2 (z) solve.
+// Dense passes (ns_dct.cu): x forward/inverse, y/z forward/inverse.
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                            cudaStream_t st);
-cudaError_t launch_dense_yz(int axis, int mode, const SpecPlan& S, double2* spec, cudaStream_t st);
+cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st);
+// Tridiagonal solve of every spectrum line along axis 1 (y) or 2 (z) (ns_dct.cu).
+cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)

@@ -6,7 +6,8 @@ pr_bc_staggered :1403-1464), its mix with periodic FFT axes, and full steps
 with wall velocity BCs (vel_bc_staggered :213-310, the banded CN-ADI of
 re_simulation_sub_tstep_interBC_combine.f90:656-701 with per-sweep faces).
 
-Tolerances: the dense trigonometric transforms round differently from the
+Tolerances: the dense trigonometric transforms and the tridiagonal line
+solves round differently from the
 oracle's scipy DCT/DST, and the wall Poisson problem is less well
 conditioned than the periodic one, so the routine bound is a relative L2 of
 1e-11; full steps keep the 1e-10 per-field bound and max|div u| <= 1e-12.
@@ -51,6 +52,10 @@ POISSON_CASES = [
     ((16, 32, 16), (1, 1, 2)),
     ((32, 24, 16), (1, 3, 3)),
     ((64, 48, 24), (1, 2, 4)),
+    ((32, 256, 16), (1, 3, 1)),
+    ((16, 32, 256), (1, 1, 2)),
+    ((32, 128, 200), (1, 4, 3)),
+    ((64, 64, 64), (3, 3, 3)),
 ]
 
 
@@ -176,7 +181,8 @@ def test_unsupported_mixes_rejected():
     from ns_3d_staggered_dp_gb300 import NSError
     bad = [
         dict(nx=32, ny=16, nz=32, bc=(2, 1, 1), pbc=(3, 1, 1)),   # wall x with periodic y/z
-        dict(nx=32, ny=256, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),  # dense y longer than 128
+        dict(nx=32, ny=1024, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),  # line-solved y longer than 512
+        dict(nx=32, ny=256, nz=32, bc=(1, 2, 2), pbc=(1, 3, 3)),   # dense y (wall z behind it) over 128
         dict(nx=24, ny=16, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),   # FFT x not a power of two
         dict(nx=25, ny=16, nz=32, bc=(2, 2, 2), pbc=(3, 3, 3)),   # odd wall x
     ]
