@@ -194,6 +194,92 @@ int ns_launch_count(const ns_handle* h, long long* launches);
 /* Version string of the library build. */
 const char* ns_version(void);
 
+/* ------------------------------------------------------------------------
+ * Batched tier: re-simulation of many sub-blocks of a parent run at once.
+ *
+ * Each subdomain is the reference's re-simulated sub-block
+ * (re_simulation_sub_tstep_interBC_combine.f90:415-811): wall velocity BCs
+ * from the parent's u* (using_Ustar), pressure BCs from the parent's dp,
+ * dp_flag = 1, the DCT pressure solve with the mean of the parent's dp, and
+ * sub_tstep sub-steps over the first parent interval with the AB2 history
+ * saved after the first sub-step and restored after the last (:443-454,
+ * :602-612).  Boundary values are taken from snapshots of the parent
+ * (big_periodic_3D.f90:664-712) and interpolated in time as MATLAB's
+ * interp1(..., 'spline') over a window of 6 snapshots
+ * (sub_tstep_BC_combined_interpolation.m:53-64).  All subdomains advance
+ * together: every stage of the step is one persistent kernel over a work
+ * queue of (subdomain, tile) items.
+ * ------------------------------------------------------------------------ */
+typedef struct ns_batch ns_batch;
+
+/* One sub-block: origin in the parent (1-based, idx_xu = x0 + (0..nx) etc.,
+ * big_periodic_3D.f90:20-25), cells, sub-steps in the first interval. */
+typedef struct ns_subdomain {
+  int x0, y0, z0;
+  int nx, ny, nz;       /* nx even; ny <= 128; nz <= 256                       */
+  int sub_tstep;        /* >= 1 (re_simulation_sub_tstep_interBC_combine.f90:104) */
+  int reserved;
+} ns_subdomain;
+
+typedef struct ns_batch_config {
+  int scheme;           /* NS_EULER or NS_AB2 (sub_tstep > 1 needs NS_AB2)      */
+  int bc;               /* velocity bc of every subdomain face: 2 or 4           */
+  int pbc;              /* pressure bc: 2, 3 or 4                                */
+  int restart;          /* 1: AB2 from the first step with the parent's history  */
+  int n_slots;          /* parent snapshots kept on the device                   */
+  int mode;             /* 0: batched launches; 1: one launch per subdomain and
+                           stage (the per-subdomain loop, for comparison)        */
+  int use_graph;        /* 1: capture each stage sequence in a CUDA graph        */
+  double nu, dt0;       /* viscosity and the parent time step                    */
+  double dx, dy, dz;    /* grid spacing (the parent's)                           */
+  int grid[16];         /* persistent CTAs per stage kernel (0: one wave);
+                           set by ns_batch_autotune                              */
+  int reserved[8];
+} ns_batch_config;
+
+void ns_batch_config_default(ns_batch_config* c);
+int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n, ns_batch** out);
+int ns_batch_destroy(ns_batch* b);
+const char* ns_batch_last_error(const ns_batch* b);
+/* cudaStream_t to enqueue on (NULL: the batch's own stream). */
+int ns_batch_set_stream(ns_batch* b, void* stream);
+
+/* Initial states: every subdomain's u, v, w, p and AB2 history from the
+ * parent session's device state (re_simulation_sub_tstep_interBC_combine.f90:421-433). */
+int ns_batch_init_from_parent(ns_batch* b, const ns_handle* parent);
+/* Host state of subdomain i (reference shapes of the subdomain; history may be NULL). */
+int ns_batch_set_state(ns_batch* b, int i, const double* u, const double* v, const double* w, const double* p,
+                       const double* hx, const double* hy, const double* hz);
+int ns_batch_get_state(ns_batch* b, int i, double* u, double* v, double* w, double* p, double* hx, double* hy,
+                       double* hz);
+
+/* Snapshot slot `slot` at parent time t: the 24 face arrays of every
+ * subdomain from the parent's last u* and dp (get_velpr_bc with using_Ustar
+ * and dp_flag = 1, NS_functions.f90:414-510, and get_pr_bc :514-562) and the
+ * mean of the parent's dp over each subdomain's interior (the mean_dp of
+ * the DCT solve, re_simulation_sub_tstep_interBC_combine.f90:766-768). */
+int ns_batch_capture(ns_batch* b, const ns_handle* parent, int slot, double t);
+/* The same snapshot from host data for subdomain i: faces in get_velpr_bc
+ * order (ns_set_faces), NULL entries zero. */
+int ns_batch_set_snapshot(ns_batch* b, int slot, double t, int i, const double* const faces[24], double mean_dp);
+
+/* Advance every subdomain over one parent interval [t0, t0 + dt0]: the
+ * first call takes sub_tstep sub-steps, later calls one step. */
+int ns_batch_advance(ns_batch* b, double t0);
+/* max|div u| over the interior of subdomain i (big_periodic_3D.f90:576-579). */
+int ns_batch_max_div(ns_batch* b, int i, double* max_div);
+int ns_batch_launch_count(const ns_batch* b, long long* launches);
+/* Time every stage kernel over a few persistent grid sizes and keep the
+ * fastest in the batch's configuration (runs steps: call on a scratch state). */
+int ns_batch_autotune(ns_batch* b, int reps);
+int ns_batch_get_config(const ns_batch* b, ns_batch_config* out);
+
+/* Weights of MATLAB interp1(knots, y, t, 'spline') (the not-a-knot cubic
+ * spline) on the window of 6 knots around t that
+ * sub_tstep_BC_combined_interpolation.m:59 takes: first = index of the
+ * window's first knot (knots ascending), value = sum_q w[q] y[first + q]. */
+int ns_spline_weights(const double* knots, int n_knots, double t, int* first, double* w);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,6 +4,8 @@ The compute path is libns_gpu.so (CUDA kernels behind a C ABI, declared in
 include/ns_gpu.h); this package only loads it and mirrors the reference's
 step interface on the host.
 """
-from .api import AB2, AB2_CN, EULER, FACE_ORDER, NSError, Session, make_config, shapes  # noqa: F401
+from .api import (AB2, AB2_CN, EULER, FACE_ORDER, Batch, NSError, Session, make_batch_config,  # noqa: F401
+                  make_config, shapes, spline_weights)
 
-__all__ = ["Session", "make_config", "shapes", "NSError", "EULER", "AB2", "AB2_CN", "FACE_ORDER"]
+__all__ = ["Session", "Batch", "make_config", "make_batch_config", "spline_weights", "shapes", "NSError", "EULER",
+           "AB2", "AB2_CN", "FACE_ORDER"]

@@ -40,6 +40,22 @@ class NSDiag(C.Structure):
                 ("euler_start_pending", C.c_int), ("reserved", C.c_int)]
 
 
+class NSSubdomain(C.Structure):
+    """Mirror of ``ns_subdomain``."""
+    _fields_ = [("x0", C.c_int), ("y0", C.c_int), ("z0", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("nz", C.c_int), ("sub_tstep", C.c_int), ("reserved", C.c_int)]
+
+
+class NSBatchConfig(C.Structure):
+    """Mirror of ``ns_batch_config``."""
+    _fields_ = [
+        ("scheme", C.c_int), ("bc", C.c_int), ("pbc", C.c_int), ("restart", C.c_int), ("n_slots", C.c_int),
+        ("mode", C.c_int), ("use_graph", C.c_int),
+        ("nu", C.c_double), ("dt0", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+        ("grid", C.c_int * 16), ("reserved", C.c_int * 8),
+    ]
+
+
 # Every entry point of include/ns_gpu.h with its ctypes signature.
 _DP = C.POINTER(C.c_double)
 SIGNATURES = {
@@ -64,6 +80,22 @@ SIGNATURES = {
     "ns_poisson_fft_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                          C.c_double, C.c_void_p]),
     "ns_version": (C.c_char_p, []),
+    "ns_batch_config_default": (None, [C.POINTER(NSBatchConfig)]),
+    "ns_batch_create": (C.c_int, [C.POINTER(NSBatchConfig), C.POINTER(NSSubdomain), C.c_int, C.POINTER(C.c_void_p)]),
+    "ns_batch_destroy": (C.c_int, [C.c_void_p]),
+    "ns_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "ns_batch_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ns_batch_init_from_parent": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ns_batch_set_state": (C.c_int, [C.c_void_p, C.c_int] + [_DP] * 7),
+    "ns_batch_get_state": (C.c_int, [C.c_void_p, C.c_int] + [_DP] * 7),
+    "ns_batch_capture": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double]),
+    "ns_batch_set_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(_DP), C.c_double]),
+    "ns_batch_advance": (C.c_int, [C.c_void_p, C.c_double]),
+    "ns_batch_max_div": (C.c_int, [C.c_void_p, C.c_int, _DP]),
+    "ns_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "ns_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
+    "ns_batch_get_config": (C.c_int, [C.c_void_p, C.POINTER(NSBatchConfig)]),
+    "ns_spline_weights": (C.c_int, [_DP, C.c_int, C.c_double, C.POINTER(C.c_int), _DP]),
 }
 
 _lib = None

@@ -198,3 +198,134 @@ class Session:
                       np.array(_f(ws, sh["w"]), order="F"))
         self._check(self.lib.ns_adi(self.h, _ptr(us), _ptr(vs), _ptr(ws)))
         return us, vs, ws
+
+
+def spline_weights(knots, t):
+    """(first, w[6]) of MATLAB interp1(knots, y, t, 'spline') on the 6-knot
+    window (ns_spline_weights): value = sum_q w[q] * y[first + q]."""
+    lib = _lib.load()
+    k = np.ascontiguousarray(knots, dtype=np.float64)
+    first = C.c_int()
+    w = np.zeros(6)
+    s = lib.ns_spline_weights(_ptr(k), len(k), float(t), C.byref(first), _ptr(w))
+    if s != 0:
+        raise NSError(s, "no 6-knot window around t")
+    return first.value, w
+
+
+def make_batch_config(**kw) -> _lib.NSBatchConfig:
+    lib = _lib.load()
+    c = _lib.NSBatchConfig()
+    lib.ns_batch_config_default(C.byref(c))
+    for k, v in kw.items():
+        if k == "grid":
+            for i, g in enumerate(v):
+                c.grid[i] = int(g)
+        else:
+            setattr(c, k, v)
+    return c
+
+
+class Batch:
+    """Batched re-simulation of sub-blocks of a parent Session (ns_batch_*).
+
+    subs: iterable of (x0, y0, z0, nx, ny, nz, sub_tstep) with 1-based
+    parent origins (idx_xu = x0 + (0..nx), big_periodic_3D.f90:20-25)."""
+
+    def __init__(self, subs, cfg=None, **kw):
+        self.lib = _lib.load()
+        self.cfg = cfg if cfg is not None else make_batch_config(**kw)
+        subs = list(subs)
+        arr = (_lib.NSSubdomain * len(subs))()
+        for i, sd in enumerate(subs):
+            x0, y0, z0, nx, ny, nz, r = sd
+            arr[i] = _lib.NSSubdomain(x0, y0, z0, nx, ny, nz, r, 0)
+        self.subs = subs
+        self.h = C.c_void_p()
+        s = self.lib.ns_batch_create(C.byref(self.cfg), arr, len(subs), C.byref(self.h))
+        if s != 0:
+            raise NSError(s, "ns_batch_create failed")
+
+    def _check(self, s):
+        if s != 0:
+            raise NSError(s, self.lib.ns_batch_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.ns_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def shapes(self, i):
+        _, _, _, nx, ny, nz, _ = self.subs[i]
+        return shapes(nx, ny, nz)
+
+    def init_from_parent(self, parent: "Session"):
+        self._check(self.lib.ns_batch_init_from_parent(self.h, parent.h))
+
+    def set_state(self, i, u, v, w, p, rhs_prev=None):
+        sh = self.shapes(i)
+        arrs = [_f(u, sh["u"]), _f(v, sh["v"]), _f(w, sh["w"]), _f(p, sh["p"])]
+        if rhs_prev is None:
+            arrs += [None] * 3
+        else:
+            arrs += [_f(rhs_prev[0], sh["u"]), _f(rhs_prev[1], sh["v"]), _f(rhs_prev[2], sh["w"])]
+        self._check(self.lib.ns_batch_set_state(self.h, i, *[_ptr(a) for a in arrs]))
+
+    def get_state(self, i, history=True):
+        sh = self.shapes(i)
+        out = {k: np.zeros(sh[k], order="F") for k in ("u", "v", "w", "p")}
+        hist = [np.zeros(sh[k], order="F") for k in ("u", "v", "w")] if history else [None] * 3
+        self._check(self.lib.ns_batch_get_state(self.h, i, _ptr(out["u"]), _ptr(out["v"]), _ptr(out["w"]),
+                                                _ptr(out["p"]), _ptr(hist[0]), _ptr(hist[1]), _ptr(hist[2])))
+        if history:
+            out["hx"], out["hy"], out["hz"] = hist
+        return out
+
+    def capture(self, parent: "Session", slot, t):
+        self._check(self.lib.ns_batch_capture(self.h, parent.h, int(slot), float(t)))
+
+    def set_snapshot(self, slot, t, i, faces: dict, mean_dp):
+        keep = []
+        arr = (C.POINTER(C.c_double) * 24)()
+        for q, k in enumerate(FACE_ORDER):
+            if k in faces and faces[k] is not None:
+                a = _f(faces[k])
+                keep.append(a)
+                arr[q] = _ptr(a)
+            else:
+                arr[q] = None
+        self._check(self.lib.ns_batch_set_snapshot(self.h, int(slot), float(t), int(i), arr, float(mean_dp)))
+
+    def advance(self, t0):
+        self._check(self.lib.ns_batch_advance(self.h, float(t0)))
+
+    def max_div(self, i):
+        d = C.c_double()
+        self._check(self.lib.ns_batch_max_div(self.h, int(i), C.byref(d)))
+        return d.value
+
+    def launch_count(self):
+        n = C.c_longlong()
+        self._check(self.lib.ns_batch_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def autotune(self, reps=3):
+        self._check(self.lib.ns_batch_autotune(self.h, int(reps)))
+        c = _lib.NSBatchConfig()
+        self._check(self.lib.ns_batch_get_config(self.h, C.byref(c)))
+        return list(c.grid)
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.lib.ns_batch_set_stream(self.h, C.c_void_p(stream_handle)))

@@ -10,6 +10,7 @@
 
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
+#include "ns_session.cuh"
 
 using namespace ns;
 
@@ -116,46 +117,59 @@ HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool 
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// The handle
-// ---------------------------------------------------------------------------
-struct ns_handle {
-  ns_config cfg;
-  Layout L;
-  cudaStream_t stream = nullptr;
-  cudaStream_t cap_stream = nullptr;  // private stream for graph capture
-  bool own_stream = false;
-  double dx, dy, dz;
-  // device fields
-  double *u = nullptr, *v = nullptr, *w = nullptr, *p = nullptr;
-  double *hx = nullptr, *hy = nullptr, *hz = nullptr;
-  double *us = nullptr, *vs = nullptr, *ws = nullptr, *dp = nullptr;
-  double *us2 = nullptr, *vs2 = nullptr, *ws2 = nullptr;  // ADI ping-pong buffers
-  double2* spec = nullptr;
-  double* inv_lam = nullptr;
-  double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
-  FftPlan plan{};
-  // ADI factors
-  double* adi_buf = nullptr;
-  LineSys sys[3][3];  // [axis][field]
-  // faces: [set 0..3][axis][field 0..3][side] -> device planes
-  double* face_buf = nullptr;
-  FaceSet faces[4]{};
-  bool face_set_nonzero[4] = {false, false, false, false};
-  unsigned long long* diag_bits = nullptr;
-  // state
-  bool first_pending = true;
-  long long steps = 0;
-  std::string err;
-  // graphs
-  cudaGraphExec_t graph = nullptr;
-  bool eager_done = false;
-  long long graph_launches = 0;
-  // launch counting and per-kernel timing (ns_profile)
-  long long launches = 0;
-  bool profiling = false;
-  std::vector<std::pair<std::string, cudaEvent_t>> prof_events;
-};
+namespace ns {
+
+// Dense transform pair of one non-periodic axis of n cells, from the MKL
+// trigonometric transforms DCT_poisson_solver applies (NS_functions.f90:1526-1625):
+//   pbc 3: F = backward staggered cosine (DCT-II / 2), G = forward staggered cosine
+//   pbc 2: sign flip of the odd (1-based) inputs, pbc-3 transform, reversal (and back)
+//   pbc 4: F = DST-I / 2 on n points, G = DST-I / (n + 1)
+// F[k][n'] (mode k from sample n'), G[n'][k] = F^-1, angles in long double.
+void dense_pair(int n, int pb, std::vector<double>& F, std::vector<double>& G) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  F.assign((size_t)n * n, 0.0);
+  G.assign((size_t)n * n, 0.0);
+  auto cosq = [&](long long m, long long q) {  // cos(pi m / q), m reduced mod 2q
+    m %= 2 * q;
+    return cosl(pi * (long double)m / (long double)q);
+  };
+  auto sinq = [&](long long m, long long q) {
+    m %= 2 * q;
+    return sinl(pi * (long double)m / (long double)q);
+  };
+  for (int k = 0; k < n; ++k)
+    for (int s = 0; s < n; ++s) {
+      long double f, g;
+      if (pb == 3 || pb == 2) {
+        const int kk = (pb == 2) ? n - 1 - k : k;  // reversal of the modes
+        const long double sg = (pb == 2 && s % 2 == 0) ? -1.0L : 1.0L;  // odd 1-based samples flipped
+        const long double cs = cosq((long long)kk * (2 * s + 1), 2LL * n);
+        f = sg * cs;
+        g = sg * cs * (kk == 0 ? 1.0L : 2.0L) / (long double)n;
+      } else {
+        const long double sn = sinq((long long)(k + 1) * (s + 1), n + 1);
+        f = sn;
+        g = 2.0L * sn / (long double)(n + 1);
+      }
+      F[(size_t)k * n + s] = (double)f;
+      G[(size_t)s * n + k] = (double)g;
+    }
+}
+
+// Eigenvalue sin^2(..)/h^2 of mode m (0-based) of one axis: FFT bins for pbc 1
+// (big_periodic_3D.f90:242-255), the trigonometric-transform modes otherwise
+// (re_simulation_sub_tstep_interBC_combine.f90:320-353).
+double axis_eig(int n, int pb, int m, double h) {
+  const double pi = 3.1415926535897932;
+  double s;
+  if (pb == 1) s = std::sin(pi * m / n);
+  else if (pb == 2) s = std::sin((m + 1) * pi / 2 / n);
+  else if (pb == 3) s = std::sin(m * pi / 2 / n);
+  else s = std::sin((m + 1) * pi / 2 / (n + 1));
+  return s * s / (h * h);
+}
+
+}  // namespace ns
 
 namespace {
 
@@ -304,11 +318,19 @@ PredictArgs predict_args(ns_handle* h) {
   a.u = h->u; a.v = h->v; a.w = h->w; a.p = h->p;
   a.us = h->us; a.vs = h->vs; a.ws = h->ws;
   a.hx = h->hx; a.hy = h->hy; a.hz = h->hz;
+  set_predict_coeffs(a, c.bc, h->dx, h->dy, h->dz, c.dt, c.nu);
+  return a;
+}
+
+}  // namespace
+
+namespace ns {
+
+void set_predict_coeffs(PredictArgs& a, const int bc[3], double dx, double dy, double dz, double dt, double nu) {
   a.one = 1.0; a.mzero = -0.0;
-  a.ulo = c.bc[0] == 1 ? 1 : 2;
-  a.vlo = c.bc[1] == 1 ? 1 : 2;
-  a.wlo = c.bc[2] == 1 ? 1 : 2;
-  const double dx = h->dx, dy = h->dy, dz = h->dz, dt = c.dt, nu = c.nu;
+  a.ulo = bc[0] == 1 ? 1 : 2;
+  a.vlo = bc[1] == 1 ? 1 : 2;
+  a.wlo = bc[2] == 1 ? 1 : 2;
   a.cx = -0.25 / dx; a.cy = -0.25 / dy; a.cz = -0.25 / dz;
   const double ix2 = 1.0 / (dx * dx), iy2 = 1.0 / (dy * dy), iz2 = 1.0 / (dz * dz);
   a.kx = nu * ix2; a.ky = nu * iy2; a.kz = nu * iz2;
@@ -320,8 +342,11 @@ PredictArgs predict_args(ns_handle* h) {
   a.dt = dt; a.e1 = 1.5 * dt; a.e2 = -0.5 * dt;
   a.gpx = -dt / dx; a.gpy = -dt / dy; a.gpz = -dt / dz;
   a.ix2 = ix2; a.iy2 = iy2; a.iz2 = iz2; a.lap0 = -2.0 * (ix2 + iy2 + iz2);
-  return a;
 }
+
+}  // namespace ns
+
+namespace {
 
 // The three sweeps with fixed buffer roles: x reads A (the predictor's
 // output) and writes B, y reads B and writes A, z reads A and writes B, so
@@ -396,56 +421,6 @@ int enqueue_step(ns_handle* h, bool first) {
   NS_CUDA(h, launch_correct(ca, h->stream));
   mark(h, "correct");
   return NS_OK;
-}
-
-// Dense transform pair of one non-periodic axis of n cells, from the MKL
-// trigonometric transforms DCT_poisson_solver applies (NS_functions.f90:1526-1625):
-//   pbc 3: F = backward staggered cosine (DCT-II / 2), G = forward staggered cosine
-//   pbc 2: sign flip of the odd (1-based) inputs, pbc-3 transform, reversal (and back)
-//   pbc 4: F = DST-I / 2 on n points, G = DST-I / (n + 1)
-// F[k][n'] (mode k from sample n'), G[n'][k] = F^-1, angles in long double.
-void dense_pair(int n, int pb, std::vector<double>& F, std::vector<double>& G) {
-  const long double pi = 3.141592653589793238462643383279502884L;
-  F.assign((size_t)n * n, 0.0);
-  G.assign((size_t)n * n, 0.0);
-  auto cosq = [&](long long m, long long q) {  // cos(pi m / q), m reduced mod 2q
-    m %= 2 * q;
-    return cosl(pi * (long double)m / (long double)q);
-  };
-  auto sinq = [&](long long m, long long q) {
-    m %= 2 * q;
-    return sinl(pi * (long double)m / (long double)q);
-  };
-  for (int k = 0; k < n; ++k)
-    for (int s = 0; s < n; ++s) {
-      long double f, g;
-      if (pb == 3 || pb == 2) {
-        const int kk = (pb == 2) ? n - 1 - k : k;  // reversal of the modes
-        const long double sg = (pb == 2 && s % 2 == 0) ? -1.0L : 1.0L;  // odd 1-based samples flipped
-        const long double cs = cosq((long long)kk * (2 * s + 1), 2LL * n);
-        f = sg * cs;
-        g = sg * cs * (kk == 0 ? 1.0L : 2.0L) / (long double)n;
-      } else {
-        const long double sn = sinq((long long)(k + 1) * (s + 1), n + 1);
-        f = sn;
-        g = 2.0L * sn / (long double)(n + 1);
-      }
-      F[(size_t)k * n + s] = (double)f;
-      G[(size_t)s * n + k] = (double)g;
-    }
-}
-
-// Eigenvalue sin^2(..)/h^2 of mode m (0-based) of one axis: FFT bins for pbc 1
-// (big_periodic_3D.f90:242-255), the trigonometric-transform modes otherwise
-// (re_simulation_sub_tstep_interBC_combine.f90:320-353).
-double axis_eig(int n, int pb, int m, double h) {
-  const double pi = 3.1415926535897932;
-  double s;
-  if (pb == 1) s = std::sin(pi * m / n);
-  else if (pb == 2) s = std::sin((m + 1) * pi / 2 / n);
-  else if (pb == 3) s = std::sin(m * pi / 2 / n);
-  else s = std::sin((m + 1) * pi / 2 / (n + 1));
-  return s * s / (h * h);
 }
 
 int build_plans(ns_handle* h) {

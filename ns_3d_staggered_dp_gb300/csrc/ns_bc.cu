@@ -3,6 +3,8 @@
 // axes including their ghosts, so edge and corner values come out as in
 // vel_bc_staggered (NS_functions.f90:213-310) and pr_bc_staggered
 // (NS_functions.f90:1403-1464).
+#include <algorithm>
+
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
 
@@ -18,10 +20,9 @@ struct AxisGeo {
 };
 
 template <int AXIS>
-__device__ __forceinline__ AxisGeo axis_geo(const Layout& L) {
+__device__ __forceinline__ AxisGeo axis_geo(const Layout& L, int t) {
   const int n1 = (AXIS == 0) ? L.ny + 2 : L.nx + 2;
   const int n2 = (AXIS == 2) ? L.ny + 2 : L.nz + 2;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   AxisGeo g;
   g.ok = t < n1 * n2;
   const int s1 = t % n1, s2 = t / n1;
@@ -67,8 +68,9 @@ __device__ __forceinline__ void vel_fill(double* x, long long st, int n, int bc,
 }
 
 template <int AXIS>
-__global__ void vel_bc_kernel(Layout L, double* us, double* vs, double* ws, FacePlanes F, int bc) {
-  const AxisGeo g = axis_geo<AXIS>(L);
+__device__ __forceinline__ void vel_bc_body(const Layout& L, double* us, double* vs, double* ws, const FacePlanes& F,
+                                            int bc, int t) {
+  const AxisGeo g = axis_geo<AXIS>(L, t);
   if (!g.ok) return;
   vel_fill(us + g.base, g.st, g.n, bc, AXIS == 0, F.f[0][0], F.f[0][1], g.plane);
   vel_fill(vs + g.base, g.st, g.n, bc, AXIS == 1, F.f[1][0], F.f[1][1], g.plane);
@@ -76,8 +78,13 @@ __global__ void vel_bc_kernel(Layout L, double* us, double* vs, double* ws, Face
 }
 
 template <int AXIS>
-__global__ void pr_bc_kernel(Layout L, double* dp, FacePlanes F, int pbc, double h) {
-  const AxisGeo g = axis_geo<AXIS>(L);
+__global__ void vel_bc_kernel(Layout L, double* us, double* vs, double* ws, FacePlanes F, int bc) {
+  vel_bc_body<AXIS>(L, us, vs, ws, F, bc, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <int AXIS>
+__device__ __forceinline__ void pr_bc_body(const Layout& L, double* dp, const FacePlanes& F, int pbc, double h, int t) {
+  const AxisGeo g = axis_geo<AXIS>(L, t);
   if (!g.ok) return;
   double* x = dp + g.base;
   const long long st = g.st;
@@ -100,11 +107,25 @@ __global__ void pr_bc_kernel(Layout L, double* dp, FacePlanes F, int pbc, double
   }
 }
 
-inline int plane_count(const Layout& L, int axis) {
-  const int n1 = (axis == 0) ? L.ny + 2 : L.nx + 2;
-  const int n2 = (axis == 2) ? L.ny + 2 : L.nz + 2;
-  return n1 * n2;
+template <int AXIS>
+__global__ void pr_bc_kernel(Layout L, double* dp, FacePlanes F, int pbc, double h) {
+  pr_bc_body<AXIS>(L, dp, F, pbc, h, blockIdx.x * blockDim.x + threadIdx.x);
 }
+
+// Batched fill pass along AXIS: velocity (PR false) or pressure ghosts, one
+// 256-element chunk of a face plane per work item.
+template <int AXIS, bool PR>
+__global__ void __launch_bounds__(256) bc_batch_kernel(const BatchBcArgs* __restrict__ tab,
+                                                       const BatchItem* __restrict__ items, int n_items) {
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    const BatchBcArgs& a = tab[w.sub];
+    const int t = w.bx * 256 + threadIdx.x;
+    if (PR) pr_bc_body<AXIS>(a.L, a.dp, a.F.ax[AXIS], a.pbc[AXIS], a.h[AXIS], t);
+    else if (a.bc[AXIS] != 3) vel_bc_body<AXIS>(a.L, a.us, a.vs, a.ws, a.F.ax[AXIS], a.bc[AXIS], t);
+  }
+}
+
 
 // Extra face slot 0 of a periodic axis (face 0 = face n) for the face field of that axis.
 __global__ void extra_slot_kernel(Layout L, double* f, int axis) {
@@ -119,6 +140,24 @@ __global__ void extra_slot_kernel(Layout L, double* f, int axis) {
 }
 
 }  // namespace
+
+int plane_count(const Layout& L, int axis) {
+  const int n1 = (axis == 0) ? L.ny + 2 : L.nx + 2;
+  const int n2 = (axis == 2) ? L.ny + 2 : L.nz + 2;
+  return n1 * n2;
+}
+
+cudaError_t launch_bc_batch(int axis, bool pr, const BatchBcArgs* tab, const BatchItem* items, int n_items, int grid,
+                            cudaStream_t st) {
+  if (n_items <= 0) return cudaSuccess;
+  grid = std::min(grid > 0 ? grid : 4 * 152, n_items);
+#define NS_BC_CASE(A, P) \
+  if (axis == A && pr == P) bc_batch_kernel<A, P><<<grid, 256, 0, st>>>(tab, items, n_items);
+  NS_BC_CASE(0, false) NS_BC_CASE(1, false) NS_BC_CASE(2, false) NS_BC_CASE(0, true) NS_BC_CASE(1, true)
+  NS_BC_CASE(2, true)
+#undef NS_BC_CASE
+  return cudaGetLastError();
+}
 
 cudaError_t launch_extra_slots(const Layout& L, double* u, double* v, double* w, const int bc[3], cudaStream_t st) {
   double* f[3] = {u, v, w};

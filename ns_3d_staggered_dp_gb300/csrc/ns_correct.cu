@@ -16,11 +16,10 @@
 
 namespace ns {
 
-__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a) {
+__device__ __forceinline__ void correct_body(const CorrectArgs& a, long long t) {
   const Layout L = a.L;
   const int nx2 = L.nx + 2, ny2 = L.ny + 2, nz2 = L.nz + 2;
   const long long tot = (long long)nx2 * ny2 * nz2;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= tot) return;
   const int i = (int)(t % nx2);
   const int j = (int)((t / nx2) % ny2);
@@ -59,6 +58,28 @@ __global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a) {
     if (a.gauge) d = fsub(c, d, dp[L.at(0, 0, 0)]);
     a.p[g] = a.dp_flag ? fadd(c, a.p[g], d) : d;
   }
+}
+
+__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a) {
+  correct_body(a, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
+
+// Batched: one 256-element chunk of a subdomain box per work item.
+__global__ void __launch_bounds__(256) correct_batch_kernel(const CorrectArgs* __restrict__ tab,
+                                                            const BatchItem* __restrict__ items, int n_items) {
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    correct_body(tab[w.sub], (long long)w.bx * 256 + threadIdx.x);
+  }
+}
+
+cudaError_t launch_correct_batch(const CorrectArgs* tab, const BatchItem* items, int n_items, int grid,
+                                 cudaStream_t st) {
+  if (n_items <= 0) return cudaSuccess;
+  grid = grid > 0 ? grid : 8 * 152;
+  if (grid > n_items) grid = n_items;
+  correct_batch_kernel<<<grid, 256, 0, st>>>(tab, items, n_items);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st) {

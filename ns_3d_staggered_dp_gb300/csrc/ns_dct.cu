@@ -48,10 +48,10 @@ __device__ __forceinline__ double rhs_cell(const DivArgs& d, const SpecPlan& S, 
 
 // x pass for a non-periodic x axis: real line -> F_x -> packed modes.
 // One warp per line (j, k); lane q computes the modes 2q' and 2q'+1.
-__global__ void __launch_bounds__(128) dense_x_fwd_kernel(SpecPlan S, DivArgs d, double2* __restrict__ spec) {
-  extern __shared__ __align__(16) double xs[];
+__device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArgs& d, double2* __restrict__ spec,
+                                                 double* xs, int bx) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int line = blockIdx.x * 4 + warp;
+  const int line = bx * 4 + warp;
   const int nx = S.nx, ny = S.ny, nz = S.nz;
   const bool valid = line < ny * nz;
   const int j = valid ? 1 + line % ny : 1, k = valid ? 1 + line / ny : 1;
@@ -75,11 +75,10 @@ __global__ void __launch_bounds__(128) dense_x_fwd_kernel(SpecPlan S, DivArgs d,
 }
 
 // x inverse for a non-periodic x axis: packed modes -> G_x -> dp slots 1..nx.
-__global__ void __launch_bounds__(128) dense_x_inv_kernel(SpecPlan S, const double2* __restrict__ spec, double* dp,
-                                                          Layout L) {
-  extern __shared__ __align__(16) double xs[];
+__device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double2* __restrict__ spec, double* dp,
+                                                 const Layout& L, double* xs, int bx) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int line = blockIdx.x * 4 + warp;
+  const int line = bx * 4 + warp;
   const int nx = S.nx, ny = S.ny, nz = S.nz;
   const bool valid = line < ny * nz;
   const int j = valid ? 1 + line % ny : 1, k = valid ? 1 + line / ny : 1;
@@ -105,14 +104,13 @@ __global__ void __launch_bounds__(128) dense_x_inv_kernel(SpecPlan S, const doub
 // Dense transform of complex lines along y (AXIS 1) or z (AXIS 2), lanes over
 // consecutive spectrum columns (coalesced).
 template <int AXIS, bool FWD>
-__global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __restrict__ spec) {
-  extern __shared__ __align__(16) double2 ls[];
+__device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __restrict__ spec, double2* ls, int bx, int by) {
   constexpr int LPC = 16, T = 8;  // 16 lines (columns) x 8 threads per line
   const int l = threadIdx.x % LPC, t = threadIdx.x / LPC;
   const int N = (AXIS == 1) ? S.ny : S.nz;
-  const int col = blockIdx.x * LPC + l;
+  const int col = bx * LPC + l;
   const bool valid = col < S.nxs;
-  const int o = blockIdx.y;  // the other index (z for y-lines, y for z-lines)
+  const int o = by;  // the other index (z for y-lines, y for z-lines)
   const long long st = (AXIS == 1) ? (long long)S.nxs : (long long)S.nxs * S.ny;
   const long long base = (AXIS == 1) ? col + (long long)S.nxs * S.ny * o : col + (long long)S.nxs * o;
   double2* line = ls + l;  // element n at line[n * LPC]
@@ -198,8 +196,9 @@ __device__ void tri_real(double* x, long long sx, int N, double sig_h2, double e
 }
 
 template <int AXIS, bool PACKED>
-__global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* __restrict__ spec) {
-  extern __shared__ __align__(16) double cm[];  // [N][TRI_T] multipliers (x2 when PACKED)
+__device__ __forceinline__ void tri_solve_body(const SpecPlan& S, double2* __restrict__ spec, double* cm, int bx,
+                                               int by) {
+  // cm: [N][TRI_T] multipliers (x2 when PACKED)
   const int l = threadIdx.x;
   const int N = AXIS == 1 ? S.ny : S.nz;
   const int n_other = AXIS == 1 ? S.nz : S.ny;
@@ -209,14 +208,14 @@ __global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* _
   const int nblk = (nreg + TRI_T - 1) / TRI_T;
   int col, o;
   bool valid;
-  if ((int)blockIdx.x < nblk) {
-    col = blockIdx.x * TRI_T + l;
-    o = blockIdx.y;
+  if (bx < nblk) {
+    col = bx * TRI_T + l;
+    o = by;
     valid = col < nreg;
   } else {
-    if ((int)blockIdx.y * TRI_T >= n_other) return;
+    if (by * TRI_T >= n_other) return;
     col = S.nxs - 1;
-    o = blockIdx.y * TRI_T + l;
+    o = by * TRI_T + l;
     valid = o < n_other;
   }
   if (!valid) return;
@@ -230,7 +229,7 @@ __global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* _
   double* cmi = PACKED ? cm + (long long)N * TRI_T + l : cmr;
   if (S.has_mean && col == 0 && o == 0) {  // the singular line
     double* x = reinterpret_cast<double*>(g);
-    tri_real(x, 2 * st, N, sr, elo, ehi, rs, cmr, true, S.mean_val);
+    tri_real(x, 2 * st, N, sr, elo, ehi, rs, cmr, true, S.mean_dev ? S.mean_val * *S.mean_dev : S.mean_val);
     tri_real(x + 1, 2 * st, N, si, elo, ehi, rs, cmi, !PACKED, 0.0);
     return;
   }
@@ -259,6 +258,85 @@ __global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* _
     p.y = fma(-cmi[j * TRI_T], p.y, x.y);
     g[(long long)j * st] = p;
   }
+}
+
+__global__ void __launch_bounds__(128) dense_x_fwd_kernel(SpecPlan S, DivArgs d, double2* __restrict__ spec) {
+  extern __shared__ __align__(16) double xs_fwd[];
+  dense_x_fwd_body(S, d, spec, xs_fwd, blockIdx.x);
+}
+__global__ void __launch_bounds__(128) dense_x_inv_kernel(SpecPlan S, const double2* __restrict__ spec, double* dp,
+                                                          Layout L) {
+  extern __shared__ __align__(16) double xs_inv[];
+  dense_x_inv_body(S, spec, dp, L, xs_inv, blockIdx.x);
+}
+template <int AXIS, bool FWD>
+__global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __restrict__ spec) {
+  extern __shared__ __align__(16) double2 ls_yz[];
+  dense_yz_body<AXIS, FWD>(S, spec, ls_yz, blockIdx.x, blockIdx.y);
+}
+template <int AXIS, bool PACKED>
+__global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* __restrict__ spec) {
+  extern __shared__ __align__(16) double cm_tri[];
+  tri_solve_body<AXIS, PACKED>(S, spec, cm_tri, blockIdx.x, blockIdx.y);
+}
+
+// ---------------------------------------------------------------------------
+// Batched passes: persistent CTAs walk (subdomain, block) work items; the
+// subdomain's arguments are staged in shared memory once per item.
+// PASS: 0 x forward, 1 x inverse, 2 y forward, 3 y inverse, 4 tridiagonal z (packed x).
+// ---------------------------------------------------------------------------
+template <int PASS>
+__global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __restrict__ tab,
+                                                         const BatchItem* __restrict__ items, int n_items) {
+  extern __shared__ __align__(16) double sm_b[];
+  __shared__ BatchSpecArgs a;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    if (threadIdx.x == 0) a = tab[w.sub];
+    __syncthreads();
+    if (PASS == 0) dense_x_fwd_body(a.S, a.d, a.spec, sm_b, w.bx);
+    if (PASS == 1) dense_x_inv_body(a.S, a.spec, a.dp, a.L, sm_b, w.bx);
+    if (PASS == 2) dense_yz_body<1, true>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);
+    if (PASS == 3) dense_yz_body<1, false>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);
+    if (PASS == 4 && threadIdx.x < TRI_T) tri_solve_body<2, true>(a.S, a.spec, sm_b, w.bx, w.by);
+    __syncthreads();
+  }
+}
+
+// Work-item grid of one pass for one subdomain.
+void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
+  gy = 1;
+  if (pass == 0 || pass == 1) gx = (S.ny * S.nz + 3) / 4;
+  else if (pass == 2 || pass == 3) { gx = (S.nxs + 15) / 16; gy = S.nz; }
+  else { gx = (S.nxs + TRI_T - 1) / TRI_T; gy = S.ny; }
+}
+
+size_t spec_pass_smem(int pass, const SpecPlan& S) {
+  if (pass == 0 || pass == 1) return (size_t)4 * S.nx * sizeof(double);
+  if (pass == 2 || pass == 3) return (size_t)S.ny * 16 * sizeof(double2);
+  return (size_t)S.nz * TRI_T * sizeof(double) * 2;
+}
+
+cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchItem* items, int n_items, size_t smem,
+                              int grid, cudaStream_t st) {
+  if (n_items <= 0) return cudaSuccess;
+  auto kern = pass == 0 ? spec_batch_kernel<0>
+            : pass == 1 ? spec_batch_kernel<1>
+            : pass == 2 ? spec_batch_kernel<2>
+            : pass == 3 ? spec_batch_kernel<3>
+                        : spec_batch_kernel<4>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  if (grid <= 0) {
+    int per_sm = 0, dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, pass == 4 ? TRI_T : 128, smem);
+    grid = (per_sm > 0 ? per_sm : 1) * nsm;
+  }
+  if (grid > n_items) grid = n_items;
+  kern<<<grid, pass == 4 ? TRI_T : 128, smem, st>>>(tab, items, n_items);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,

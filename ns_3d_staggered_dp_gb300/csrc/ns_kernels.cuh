@@ -4,6 +4,13 @@
 
 namespace ns {
 
+// One work item of a batched launch: a subdomain and the block coordinates
+// of one CTA's worth of work in that subdomain.  Persistent CTAs walk an
+// array of items (item blockIdx.x, then + gridDim.x, ...).
+struct BatchItem {
+  int sub, bx, by, bz;
+};
+
 // Called after every kernel launch with the kernel's name (launch counting
 // and per-kernel event timing in ns_api.cu).
 struct Marker {
@@ -74,6 +81,11 @@ __device__ __forceinline__ double predictor_combine(const PredictArgs& a, const 
 
 size_t predict_smem_bytes();
 cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st);
+// Predictor tiles of one box (work items of the batched launch).
+void predict_tiles(const Layout& L, int& gx, int& gy, int& gz);
+// Batched predictor over the items (grid <= 0: one wave of resident CTAs).
+cudaError_t launch_predict_batch(const PredictArgs* tab, const BatchItem* items, int n_items, int scheme, bool first,
+                                 bool dpf, int grid, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Boundary fills (ns_bc.cu)
@@ -96,6 +108,23 @@ cudaError_t launch_extra_slots(const Layout& L, double* u, double* v, double* w,
 // pr_bc_staggered (NS_functions.f90:1403-1464), the three axis passes.
 cudaError_t launch_pr_bc(const Layout& L, double* dp, const FaceSet& F, const int pbc[3], double dx, double dy,
                          double dz, cudaStream_t st);
+// Elements of the face plane normal to an axis (ghosts included).
+int plane_count(const Layout& L, int axis);
+// Per-subdomain arguments of the batched fills.
+struct BatchBcArgs {
+  Layout L;
+  double* us;
+  double* vs;
+  double* ws;
+  double* dp;
+  FaceSet F;
+  int bc[3], pbc[3];
+  double h[3];
+};
+// One axis pass of vel_bc_staggered (pr false) or pr_bc_staggered (pr true)
+// over the items (sub, 256-element chunk bx of the plane).
+cudaError_t launch_bc_batch(int axis, bool pr, const BatchBcArgs* tab, const BatchItem* items, int n_items, int grid,
+                            cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // ADI (ns_adi.cu)
@@ -142,6 +171,7 @@ struct FftPlan {
   const double* inv[3];   // dense inverse matrices (x: G^T [k][n]; y, z: G [n][k])
   int has_mean;           // 1: the singular mode is set to mean_val (after the forward passes)
   double mean_val;        // FFT z solve: the singular entry; tridiagonal solve: the singular line's mean
+  const double* mean_dev; // non-null: the line mean is mean_val * (*mean_dev) (a mean_dp set on the device)
   // Tridiagonal solve along the wall axis s, one line per (x mode, other-axis mode):
   // rows (p[j-1] - (2 - e_j - sigma h^2) p[j] + p[j+1]) = h^2 scale rhs[j].
   const double* eig_x;    // lambda of the x modes (nxs entries; 2 per entry when x is packed)
@@ -194,6 +224,19 @@ cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double
 cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st);
 // Tridiagonal solve of every spectrum line along axis 1 (y) or 2 (z) (ns_dct.cu).
 cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st);
+// Batched spectral passes of all-wall boxes (x dense packed, y dense, z line solve).
+struct BatchSpecArgs {
+  SpecPlan S;
+  DivArgs d;
+  double2* spec;
+  double* dp;
+  Layout L;
+};
+// pass: 0 x forward (divergence + BC terms), 1 x inverse, 2 y forward, 3 y inverse, 4 z line solve.
+void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy);
+size_t spec_pass_smem(int pass, const SpecPlan& S);
+cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchItem* items, int n_items, size_t smem,
+                              int grid, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)
@@ -215,6 +258,9 @@ struct CorrectArgs {
   double one, mzero;
 };
 cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st);
+// Batched correction over the items (sub, 256-element chunk bx of the box).
+cudaError_t launch_correct_batch(const CorrectArgs* tab, const BatchItem* items, int n_items, int grid,
+                                 cudaStream_t st);
 
 // max|div u| over the interior and probe value (diagnostic).
 cudaError_t launch_diag(const Layout& L, const double* u, const double* v, const double* w, double idx, double idy,

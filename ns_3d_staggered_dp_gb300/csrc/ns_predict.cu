@@ -20,6 +20,8 @@
 // FP64 warp instruction costs its full issue slot however many lanes are
 // active, so no halo work is done by single lanes of the row warps.
 // Every FP64 operation is issued in FMA form (see ns_internal.cuh).
+#include <algorithm>
+
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
 
@@ -113,17 +115,16 @@ __device__ __forceinline__ void products_zface(PredSmem& S, const FOne& c, int x
 }  // namespace
 
 // MODE: 0 predictor, 1 conv only (writes conv into us/vs/ws), 2 diffusion only.
+// One tile (bx, by) of TX x TY faces marching over the z-chunk bz.
 template <int SCHEME, bool FIRST, bool DPF, int MODE>
-__global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  PredSmem& S = *reinterpret_cast<PredSmem*>(smem_raw);
+__device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, int bx, int by, int bz) {
   const Layout L = a.L;
   const FOne c{a.one, a.mzero};
   const int lane = threadIdx.x;
   const int wy = threadIdx.y;  // 0..TY
-  const int i0 = 1 + TX * blockIdx.x;
-  const int j0 = 1 + TY * blockIdx.y;
-  const int k0 = 1 + KC * blockIdx.z;
+  const int i0 = 1 + TX * bx;
+  const int j0 = 1 + TY * by;
+  const int k0 = 1 + KC * bz;
   const int k1 = min(k0 + KC, L.nz + 1);
   // smem coordinates of this thread's position: x = i0-1+lane+1 -> xa = lane+1; y = j0-1+wy -> yb = wy
   const int xa = lane + 1;
@@ -242,6 +243,27 @@ __global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
   }
 }
 
+template <int SCHEME, bool FIRST, bool DPF, int MODE>
+__global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  predict_body<SCHEME, FIRST, DPF, MODE>(a, *reinterpret_cast<PredSmem*>(smem_raw), blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Batched: persistent CTAs walk the work items (subdomain, tile) of a batch.
+template <int SCHEME, bool FIRST, bool DPF>
+__global__ void __launch_bounds__(TX*(TY + 1)) predict_batch_kernel(const PredictArgs* __restrict__ tab,
+                                                                    const BatchItem* __restrict__ items, int n_items) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ PredictArgs a;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    if (threadIdx.x == 0 && threadIdx.y == 0) a = tab[w.sub];
+    __syncthreads();
+    predict_body<SCHEME, FIRST, DPF, 0>(a, *reinterpret_cast<PredSmem*>(smem_raw), w.bx, w.by, w.bz);
+    __syncthreads();
+  }
+}
+
 size_t predict_smem_bytes() { return sizeof(PredSmem); }
 
 template <int SCHEME, bool FIRST, bool DPF, int MODE>
@@ -264,6 +286,41 @@ cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dp
   NS_PRED_CASE(0, false, false) NS_PRED_CASE(0, false, true) NS_PRED_CASE(0, true, false) NS_PRED_CASE(0, true, true)
   NS_PRED_CASE(1, false, false) NS_PRED_CASE(1, false, true) NS_PRED_CASE(1, true, false) NS_PRED_CASE(1, true, true)
   NS_PRED_CASE(2, false, false) NS_PRED_CASE(2, false, true) NS_PRED_CASE(2, true, false) NS_PRED_CASE(2, true, true)
+#undef NS_PRED_CASE
+  return cudaErrorInvalidValue;
+}
+
+void predict_tiles(const Layout& L, int& gx, int& gy, int& gz) {
+  gx = (L.nx + TX - 1) / TX;
+  gy = (L.ny + TY - 1) / TY;
+  gz = (L.nz + KC - 1) / KC;
+}
+
+template <int SCHEME, bool FIRST, bool DPF>
+static cudaError_t launch_bt(const PredictArgs* tab, const BatchItem* items, int n_items, int grid, cudaStream_t st) {
+  auto kern = predict_batch_kernel<SCHEME, FIRST, DPF>;
+  const size_t sm = sizeof(PredSmem);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  if (grid <= 0) {
+    int per_sm = 0, dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TX * (TY + 1), sm);
+    grid = std::max(1, per_sm) * nsm;
+  }
+  grid = std::min(grid, n_items);
+  if (grid <= 0) return cudaSuccess;
+  kern<<<grid, dim3(TX, TY + 1), sm, st>>>(tab, items, n_items);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_predict_batch(const PredictArgs* tab, const BatchItem* items, int n_items, int scheme, bool first,
+                                 bool dpf, int grid, cudaStream_t st) {
+#define NS_PRED_CASE(S, F, D) \
+  if (scheme == S && first == F && dpf == D) return launch_bt<S, F, D>(tab, items, n_items, grid, st);
+  NS_PRED_CASE(0, false, false) NS_PRED_CASE(0, false, true) NS_PRED_CASE(0, true, false) NS_PRED_CASE(0, true, true)
+  NS_PRED_CASE(1, false, false) NS_PRED_CASE(1, false, true) NS_PRED_CASE(1, true, false) NS_PRED_CASE(1, true, true)
 #undef NS_PRED_CASE
   return cudaErrorInvalidValue;
 }

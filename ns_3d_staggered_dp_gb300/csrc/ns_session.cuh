@@ -1,0 +1,59 @@
+// The session handle of libns_gpu.so (shared by the session tier, ns_api.cu,
+// and the batched tier, ns_batch.cu, which reads a parent session's fields).
+#pragma once
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/ns_gpu.h"
+#include "ns_internal.cuh"
+#include "ns_kernels.cuh"
+
+struct ns_handle {
+  ns_config cfg;
+  ns::Layout L;
+  cudaStream_t stream = nullptr;
+  cudaStream_t cap_stream = nullptr;  // private stream for graph capture
+  bool own_stream = false;
+  double dx, dy, dz;
+  // device fields
+  double *u = nullptr, *v = nullptr, *w = nullptr, *p = nullptr;
+  double *hx = nullptr, *hy = nullptr, *hz = nullptr;
+  double *us = nullptr, *vs = nullptr, *ws = nullptr, *dp = nullptr;
+  double *us2 = nullptr, *vs2 = nullptr, *ws2 = nullptr;  // ADI ping-pong buffers
+  double2* spec = nullptr;
+  double* inv_lam = nullptr;
+  double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
+  ns::FftPlan plan{};
+  // ADI factors
+  double* adi_buf = nullptr;
+  ns::LineSys sys[3][3];  // [axis][field]
+  // faces: [set 0..3][axis][field 0..3][side] -> device planes
+  double* face_buf = nullptr;
+  ns::FaceSet faces[4]{};
+  bool face_set_nonzero[4] = {false, false, false, false};
+  unsigned long long* diag_bits = nullptr;
+  // state
+  bool first_pending = true;
+  long long steps = 0;
+  std::string err;
+  // graphs
+  cudaGraphExec_t graph = nullptr;
+  bool eager_done = false;
+  long long graph_launches = 0;
+  // launch counting and per-kernel timing (ns_profile)
+  long long launches = 0;
+  bool profiling = false;
+  std::vector<std::pair<std::string, cudaEvent_t>> prof_events;
+};
+
+
+namespace ns {
+// Dense transform pair (forward F [k][n], inverse G [n][k]) of one wall axis
+// of n cells with pressure code pb (ns_api.cu).
+void dense_pair(int n, int pb, std::vector<double>& F, std::vector<double>& G);
+// sin^2(..)/h^2 of mode m of one axis (pbc 1 FFT bin, else the trigonometric mode).
+double axis_eig(int n, int pb, int m, double h);
+// Predictor coefficients of a box with velocity codes bc (ns_api.cu).
+void set_predict_coeffs(PredictArgs& a, const int bc[3], double dx, double dy, double dz, double dt, double nu);
+}  // namespace ns

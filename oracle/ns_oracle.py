@@ -1018,3 +1018,66 @@ def run(st, cfg, nsteps, faces=None, solver="auto"):
     for _ in range(nsteps):
         st = step(st, cfg, faces=faces, cnf=cnf, solver=solver)
     return st
+
+
+# ---------------------------------------------------------------------------
+# Sub-block re-simulation -- re_simulation_sub_tstep_interBC_combine.f90:415-811
+# ---------------------------------------------------------------------------
+def spline_window(knot_t, t, tol=1e-12):
+    """First index of the 6 knots interp1 uses around t
+    (sub_tstep_BC_combined_interpolation.m:59: the last knot <= t, two before it,
+    three after it)."""
+    k = np.nonzero(np.asarray(knot_t) <= t + tol)[0]
+    if k.size == 0:
+        raise ValueError("t before the first knot")
+    first = int(k[-1]) - 2
+    if first < 0 or first + 6 > len(knot_t):
+        raise ValueError("no 6-knot window around t")
+    return first
+
+
+def interp_spline(knot_t, knot_vals, t, tol=1e-12):
+    """interp1(t0(win), y(win, ...), t, 'spline'): not-a-knot cubic spline over
+    the 6-knot window, elementwise over the arrays in knot_vals."""
+    from scipy.interpolate import CubicSpline
+    kt = np.asarray(knot_t, dtype=float)
+    at = np.nonzero(np.abs(kt - t) <= tol)[0]
+    if at.size:  # a knot: the data value
+        return np.array(knot_vals[int(at[0])], copy=True)
+    f = spline_window(kt, t, tol)
+    y = np.stack([knot_vals[f + q] for q in range(6)], axis=0)
+    return CubicSpline(kt[f:f + 6], y, axis=0, bc_type="not-a-knot")(t)
+
+
+def resimulate(st, cfg, knot_t, knot_data, t_start, n_intervals, sub_tstep=1, restart=False):
+    """Re-simulate one sub-block driven by parent data.
+
+    ``knot_data[k] = (u_star_sub, v_star_sub, w_star_sub, dp_sub)`` is the
+    parent's sub-block at time ``knot_t[k]`` (the HDF5 groups of
+    big_periodic_3D.f90:664-712).  Each step takes the spline-interpolated
+    u*/dp sub-blocks at its end time (:496-504), builds the faces with
+    get_velpr_bc (using_Ustar, dp_flag = 1; :510-520) and steps with the
+    DCT pressure solve whose mean is the interpolated dp's interior mean
+    (:766-768).  The first parent interval is covered by ``sub_tstep``
+    sub-steps with the AB2 history saved after the first and restored after
+    the last (:443-454, :602-612).  ``st.first`` is the Euler start
+    (``not restart``, :565).
+    """
+    dx, dy, dz = cfg.h
+    st = st.copy()
+    st.first = not restart
+    saved = None
+    for m in range(n_intervals):
+        nsub = sub_tstep if m == 0 else 1
+        dt = cfg.dt / nsub
+        for s in range(1, nsub + 1):
+            t = t_start + (s * dt if m == 0 else (m + 1) * cfg.dt)
+            u_s, v_s, w_s, dp_s = (interp_spline(knot_t, [kd[q] for kd in knot_data], t) for q in range(4))
+            faces = get_velpr_bc(u_s, v_s, w_s, dp_s, cfg.bc, cfg.pbc, dx, dy, dz, dt, 1, True, None)
+            c = dataclasses.replace(cfg, dt=dt, mean_dp=float(np.mean(dp_s[1:-1, 1:-1, 1:-1])), gauge=0, dp_flag=1)
+            st = step(st, c, faces=faces)
+            if nsub > 1 and s == 1:
+                saved = (st.px.copy(), st.py.copy(), st.pz.copy())
+            if nsub > 1 and s == nsub:
+                st.px, st.py, st.pz = (a.copy() for a in saved)
+    return st
