@@ -280,6 +280,38 @@ int ns_batch_get_config(const ns_batch* b, ns_batch_config* out);
  * window's first knot (knots ascending), value = sum_q w[q] y[first + q]. */
 int ns_spline_weights(const double* knots, int n_knots, double t, int* first, double* w);
 
+/* ------------------------------------------------------------------------
+ * Adjoint tier: the discrete adjoint of the periodic step.
+ *
+ * The reference has no adjoint; this is the transpose of the tangent-linear
+ * model of the step above (big_periodic_3D.f90:326-567) on a triply
+ * periodic box with dp_flag = 0, for NS_AB2_CN, NS_AB2 and NS_EULER:
+ * projection (symmetric), the CN-ADI sweeps with the transposed line
+ * systems in the order z, y, x, and the convection linearised about the
+ * stored forward velocity.  The control is the set of independent periodic
+ * values of u, v, w: every entry that is a periodic copy (u(nx+1,:,:),
+ * the ghost rows of the cell axes) is an image of another entry.
+ * ------------------------------------------------------------------------ */
+
+/* Run nsteps steps from the current state (as ns_step), keeping the state
+ * at steps 0, K, 2K, ... (K = ckpt_every) on the device.  The state after
+ * the call is the state after nsteps steps.  Device memory: 6 fields per
+ * checkpoint plus 3 per step of a segment of K steps. */
+int ns_adj_forward(ns_handle* h, int nsteps, int ckpt_every);
+
+/* Gradient of a function J of the final velocity with respect to the
+ * initial one, given dJ/du(T), dJ/dv(T), dJ/dw(T) (host, reference shapes;
+ * an entry that is a periodic copy adds into the value it copies).  Each
+ * segment of K steps is recomputed from its checkpoint and then stepped
+ * back.  grad_u/v/w (host, reference shapes) receive dJ/du0 etc. on the
+ * independent entries and 0 on the periodic copies; grad_hx/hy/hz (may be
+ * NULL) receive dJ/d(rhs_?_previous) of the initial history (0 after an
+ * Euler start).  The session state is restored to the state after the
+ * forward run.  NS_ERR_UNSUPPORTED_BC unless bc = pbc = 1 on every axis
+ * and dp_flag = 0. */
+int ns_adj_backward(ns_handle* h, const double* dJ_du, const double* dJ_dv, const double* dJ_dw, double* grad_u,
+                    double* grad_v, double* grad_w, double* grad_hx, double* grad_hy, double* grad_hz);
+
 #ifdef __cplusplus
 }
 #endif

@@ -199,6 +199,26 @@ class Session:
         self._check(self.lib.ns_adi(self.h, _ptr(us), _ptr(vs), _ptr(ws)))
         return us, vs, ws
 
+    # adjoint tier ------------------------------------------------------------
+    def adj_forward(self, nsteps, ckpt_every):
+        """Run nsteps steps keeping a checkpoint every ckpt_every steps (ns_adj_forward)."""
+        self._check(self.lib.ns_adj_forward(self.h, int(nsteps), int(ckpt_every)))
+
+    def adj_backward(self, dJ_du, dJ_dv, dJ_dw, history=False):
+        """Gradient of J(u(T)) with respect to the initial u, v, w (ns_adj_backward).
+
+        Returns {"u", "v", "w"} (and "hx", "hy", "hz" with history=True) in the
+        reference shapes, zero on the entries that are periodic copies."""
+        sh = self.shapes
+        seeds = [_f(dJ_du, sh["u"]), _f(dJ_dv, sh["v"]), _f(dJ_dw, sh["w"])]
+        out = {k: np.zeros(sh[k], order="F") for k in ("u", "v", "w")}
+        hist = [np.zeros(sh[k], order="F") for k in ("u", "v", "w")] if history else [None] * 3
+        self._check(self.lib.ns_adj_backward(self.h, *[_ptr(a) for a in seeds], _ptr(out["u"]), _ptr(out["v"]),
+                                             _ptr(out["w"]), _ptr(hist[0]), _ptr(hist[1]), _ptr(hist[2])))
+        if history:
+            out["hx"], out["hy"], out["hz"] = hist
+        return out
+
 
 def spline_weights(knots, t):
     """(first, w[6]) of MATLAB interp1(knots, y, t, 'spline') on the 6-knot

@@ -50,7 +50,10 @@ std::vector<double> thomas_solve(const HostLineSys& S, std::vector<double> r) {
 // CN system of one sweep axis (mat_CN, NS_functions.f90:1245-1294).
 // normal: the swept field is staggered along the axis (A matrix, n+1
 // unknowns); otherwise tangential (B matrix, n+2 unknowns).
-HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool normal, int closure) {
+// transposed (periodic only): the system M^T of the adjoint sweep, whose
+// corner entries are those of M exchanged.
+HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool normal, int closure,
+                            bool transposed = false) {
   const double idx2 = 1.0 / (h * h);
   const double dg = 1.0 + 0.5 * dt * nu * 2.0 * idx2;
   const double of = -0.5 * dt * nu * 1.0 * idx2;
@@ -65,6 +68,7 @@ HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool 
       b[0] = dg + of;
       tr = 0.0;
     }
+    if (transposed) std::swap(tr, bl);
     const double gam = -b[0];
     b[0] -= gam;
     b[n - 1] -= tr * bl / gam;
@@ -565,39 +569,47 @@ int build_plans(ns_handle* h) {
 
 constexpr int kAdiPad = 8;  // zero padding on each side of the factor tables
 
-int build_adi(ns_handle* h) {
+// Factor tables of the nine line systems (3 sweeps x 3 fields) in one device
+// buffer *buf; transposed: the systems of the adjoint sweeps.
+int build_line_tables(ns_handle* h, bool transposed, LineSys sys[3][3], double** buf) {
   const ns_config& c = h->cfg;
-  if (c.scheme != NS_AB2_CN) return NS_OK;
   const int ns_[3] = {c.nx, c.ny, c.nz};
   const double hs[3] = {h->dx, h->dy, h->dz};
   HostLineSys hs_sys[3][3];
   size_t total = 0;
   for (int ax = 0; ax < 3; ++ax)
     for (int f = 0; f < 3; ++f) {
-      hs_sys[ax][f] = build_cn_system(ns_[ax], c.bc[ax], hs[ax], c.dt, c.nu, f == ax, c.cn_periodic_closure);
+      hs_sys[ax][f] =
+          build_cn_system(ns_[ax], c.bc[ax], hs[ax], c.dt, c.nu, f == ax, c.cn_periodic_closure, transposed);
       total += (hs_sys[ax][f].l.size() + 2 * kAdiPad) * 3 + hs_sys[ax][f].z.size();
     }
-  NS_CUDA(h, cudaMalloc(&h->adi_buf, total * sizeof(double)));
+  NS_CUDA(h, cudaMalloc(buf, total * sizeof(double)));
   std::vector<double> host(total, 0.0);
   size_t off = 0;
   for (int ax = 0; ax < 3; ++ax)
     for (int f = 0; f < 3; ++f) {
       const HostLineSys& S = hs_sys[ax][f];
-      LineSys& D = h->sys[ax][f];
+      LineSys& D = sys[ax][f];
       const size_t m = S.l.size(), mp = m + 2 * kAdiPad;
-      std::memcpy(&host[off + kAdiPad], S.l.data(), m * sizeof(double)); D.l = h->adi_buf + off; off += mp;
-      std::memcpy(&host[off + kAdiPad], S.dinv.data(), m * sizeof(double)); D.dinv = h->adi_buf + off; off += mp;
-      std::memcpy(&host[off + kAdiPad], S.cu.data(), m * sizeof(double)); D.cu = h->adi_buf + off; off += mp;
-      std::memcpy(&host[off], S.z.data(), S.z.size() * sizeof(double)); D.z = h->adi_buf + off; off += S.z.size();
+      std::memcpy(&host[off + kAdiPad], S.l.data(), m * sizeof(double)); D.l = *buf + off; off += mp;
+      std::memcpy(&host[off + kAdiPad], S.dinv.data(), m * sizeof(double)); D.dinv = *buf + off; off += mp;
+      std::memcpy(&host[off + kAdiPad], S.cu.data(), m * sizeof(double)); D.cu = *buf + off; off += mp;
+      std::memcpy(&host[off], S.z.data(), S.z.size() * sizeof(double)); D.z = *buf + off; off += S.z.size();
       D.s0 = S.s0; D.s1 = S.s1; D.zA = S.zA; D.zB = S.zB; D.lo = S.lo; D.hi = S.hi;
       D.periodic = S.periodic; D.n = S.n; D.pad = kAdiPad;
     }
-  NS_CUDA(h, cudaMemcpyAsync(h->adi_buf, host.data(), total * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  NS_CUDA(h, cudaMemcpyAsync(*buf, host.data(), total * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
   return NS_OK;
 }
 
+int build_adi(ns_handle* h) {
+  if (h->cfg.scheme != NS_AB2_CN) return NS_OK;
+  return build_line_tables(h, false, h->sys, &h->adi_buf);
+}
+
 void free_all(ns_handle* h) {
+  ns::api_free_adjoint(h);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   double* bufs[] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz, h->us, h->vs, h->ws, h->dp, h->inv_lam, h->adi_buf, h->face_buf,
                     h->us2, h->vs2, h->ws2};
@@ -611,6 +623,22 @@ void free_all(ns_handle* h) {
 }
 
 }  // namespace
+
+// Session internals shared with the adjoint tier (ns_adjoint.cu).
+namespace ns {
+int api_fail(ns_handle* h, int code, const std::string& msg) { return fail(h, code, msg); }
+cudaError_t api_h2d_field(ns_handle* h, double* dst, const double* src, int field) {
+  return h2d_field(h, dst, src, field);
+}
+cudaError_t api_d2h_field(ns_handle* h, double* dst, const double* src, int field) {
+  return d2h_field(h, dst, src, field);
+}
+void api_mark(ns_handle* h, const char* name, int nkernels) { mark(h, name, nkernels); }
+Marker api_marker(ns_handle* h) { return marker(h); }
+int api_build_line_tables(ns_handle* h, bool transposed, LineSys sys[3][3], double** buf) {
+  return build_line_tables(h, transposed, sys, buf);
+}
+}  // namespace ns
 
 extern "C" {
 

@@ -9,6 +9,10 @@
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
 
+namespace ns {
+struct AdjState;  // discrete adjoint tier (ns_adjoint.cu)
+}
+
 struct ns_handle {
   ns_config cfg;
   ns::Layout L;
@@ -45,7 +49,20 @@ struct ns_handle {
   long long launches = 0;
   bool profiling = false;
   std::vector<std::pair<std::string, cudaEvent_t>> prof_events;
+  // adjoint tier: checkpoints, stored inputs and adjoint fields (owned by ns_adjoint.cu)
+  ns::AdjState* adj = nullptr;
 };
+
+namespace ns {
+// Session internals shared by ns_api.cu and ns_adjoint.cu.
+int api_fail(ns_handle* h, int code, const std::string& msg);
+cudaError_t api_h2d_field(ns_handle* h, double* dst, const double* src, int field);
+cudaError_t api_d2h_field(ns_handle* h, double* dst, const double* src, int field);
+void api_mark(ns_handle* h, const char* name, int nkernels);
+Marker api_marker(ns_handle* h);
+int api_build_line_tables(ns_handle* h, bool transposed, LineSys sys[3][3], double** buf);
+void api_free_adjoint(ns_handle* h);
+}  // namespace ns
 
 
 namespace ns {
