@@ -408,6 +408,150 @@ def run_resim(args):
     return 0
 
 
+def _slots(a, which, n):
+    """Independent values of a periodic reference-shaped field."""
+    sl = {"u": (slice(0, n), slice(1, n + 1), slice(1, n + 1)), "v": (slice(1, n + 1), slice(0, n), slice(1, n + 1)),
+          "w": (slice(1, n + 1), slice(1, n + 1), slice(0, n))}[which]
+    return a[sl]
+
+
+def _embed(A, which, n):
+    shp = {"u": (n + 1, n + 2, n + 2), "v": (n + 2, n + 1, n + 2), "w": (n + 2, n + 2, n + 1)}[which]
+    out = np.zeros(shp, order="F")
+    _slots(out, which, n)[...] = A
+    return out
+
+
+def _expand(A, which, n):
+    face, cell = np.r_[np.arange(n), 0], np.r_[n - 1, np.arange(n), 0]
+    ix = {"u": (face, cell, cell), "v": (cell, face, cell), "w": (cell, cell, face)}[which]
+    return np.asfortranarray(A[np.ix_(*ix)])
+
+
+def run_adjoint(args):
+    """Gradient of J = 1/2 |u(T) - u_target|^2 over the central 64^3 of a 128^3
+    periodic box with respect to the initial velocity: T = 50 AB2-CN steps
+    (nu = 1/1600, dt from CFL 0.3), checkpoint every 10 steps.  The initial
+    field has the decaying-turbulence spectrum (seed 2024); u_target is the
+    forward run from the initial field plus 0.1 x a second field (seed 5).
+    Reports the backward pass's cell-steps/s, its cost per step against a
+    plain forward step, and central differences of J of the forward run in
+    32 seeded directions against the gradient."""
+    import torch
+    from ns_3d_staggered_dp_gb300 import Session, make_config
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    n, T, K = 128, args.adj_steps, args.adj_ckpt
+    nu = 1.0 / 1600.0
+    u, v, w, p, umax = hit_initial_field(n, seed=2024)
+    u5, v5, w5, _, _ = hit_initial_field(n, seed=5)
+    dt = 0.3 * (2 * np.pi / n) / umax
+    ncell = n ** 3
+    lo, hi = n // 4, 3 * n // 4
+    reg = (slice(lo, hi),) * 3
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    with Session(make_config(n, n, n, nu=nu, dt=dt, scheme=2)) as s:
+        s.set_stream(stream.cuda_stream)
+
+        def final_slots():
+            o = s.get_state(history=False)
+            return [np.ascontiguousarray(_slots(o[k], k, n)) for k in "uvw"]
+
+        def J_of(U, tgt):
+            return 0.5 * sum(float(np.sum((U[q][reg] - tgt[q][reg]) ** 2)) for q in range(3))
+
+        # target: forward run from the perturbed field
+        s.set_state(u + 0.1 * u5, v + 0.1 * v5, w + 0.1 * w5, p)
+        s.step(T)
+        tgt = final_slots()
+        # plain forward step time (graph replay, CUDA events)
+        s.set_state(u, v, w, p)
+        s.step(3)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(T)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fwd_ms = e0.elapsed_time(e1) / T
+        # warm run of the adjoint pair (allocations, graph capture)
+        s.set_state(u, v, w, p)
+        s.adj_forward(T, K)
+        UT = final_slots()
+        # seed and gradient in pinned host memory
+        sh = s.shapes
+        pin = lambda shp: torch.zeros(int(np.prod(shp)), dtype=torch.float64, pin_memory=True).numpy().reshape(
+            shp, order="F")
+        seed = [pin(sh[k]) for k in "uvw"]
+        gout = {k: pin(sh[k]) for k in "uvw"}
+        for q, k in enumerate("uvw"):
+            g = np.zeros_like(UT[q])
+            g[reg] = UT[q][reg] - tgt[q][reg]
+            seed[q][...] = _embed(g, k, n)
+        s.adj_backward(*seed, out=gout)
+        # timed: forward with checkpoints, then the backward pass
+        l0 = s.launch_count()
+        s.set_state(u, v, w, p)
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            t0 = time.perf_counter()
+            s.adj_forward(T, K)
+            t1 = time.perf_counter()
+            grad = s.adj_backward(*seed, out=gout)
+            t2 = time.perf_counter()
+        launches = s.launch_count() - l0
+        fwdk_ms, bwd_ms = 1e3 * (t1 - t0) / T, 1e3 * (t2 - t1) / T
+        J0 = J_of(final_slots(), tgt)
+        # central differences of the forward run in seeded directions
+        G = [np.ascontiguousarray(_slots(grad[k], k, n)) for k in "uvw"]
+        rng = np.random.default_rng(5)
+        rms = float(np.sqrt(np.mean(_slots(u, "u", n) ** 2)))
+        eps = args.adj_eps * rms
+        base = [np.ascontiguousarray(_slots(a, k, n)) for a, k in zip((u, v, w), "uvw")]
+        errs = []
+        t_fd = time.perf_counter()
+        for _ in range(args.adj_dirs):
+            d = [rng.standard_normal((n, n, n)) for _ in range(3)]
+            Js = []
+            for sg in (1.0, -1.0):
+                f = [_expand(b + sg * eps * dd, k, n) for b, dd, k in zip(base, d, "uvw")]
+                s.set_state(f[0], f[1], f[2], p)
+                s.step(T)
+                Js.append(J_of(final_slots(), tgt))
+            fd = (Js[0] - Js[1]) / (2 * eps)
+            ad = sum(float(np.vdot(Gq, dq)) for Gq, dq in zip(G, d))
+            errs.append(abs(fd - ad) / abs(ad))
+        fd_sec = time.perf_counter() - t_fd
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "FP64 adjoint cell-steps/s (dJ/du0 over 50 AB2-CN steps of a 128^3 periodic box, checkpoint every 10)",
+        "value": ncell * T / (bwd_ms * T / 1e3), "unit": UNIT, "n_gpus": world, "steps": T, "warmup": 1,
+        "ms_per_step": bwd_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded k^4 exp(-2(k/4)^2) initial field, seed 2024; target from + 0.1 x seed 5 field)",
+        "config": {"workload": "adjoint: J = 1/2 |u(T) - u_target|^2 over the central 64^3 of a 128^3 periodic box",
+                   "grid": [n, n, n], "scheme": "AB2-CN", "nu": nu, "dt": dt, "steps": T, "ckpt_every": K,
+                   "l2": "state 7 x 19 MB, checkpoints and stored inputs > L2 in total"},
+        "forward_ms_per_step": fwd_ms,
+        "forward_with_checkpoints_ms_per_step": fwdk_ms,
+        "backward_ms_per_step": bwd_ms,
+        "adjoint_cost_vs_forward": bwd_ms / fwd_ms,
+        "gradient_run_cost_vs_forward": (fwdk_ms + bwd_ms) / fwd_ms,
+        "J": J0,
+        "fd_check": {"directions": args.adj_dirs, "eps": eps, "max_rel_err": max(errs) if errs else None,
+                     "median_rel_err": float(np.median(errs)) if errs else None, "seconds": fd_sec},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "e2e": {"value": ncell * T / (t2 - t0), "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * (n + 1) * (n + 2) ** 2 / T,
+                "d2h_bytes_per_step": 3 * 8 * (n + 1) * (n + 2) ** 2 / T,
+                "path": "ns_adj_forward + ns_adj_backward (pinned host seed in, pinned host gradient out)"},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
 
@@ -558,11 +702,17 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--ref-budget-s", type=float, default=60.0)
-    ap.add_argument("--workload", default="hit", choices=["hit", "channel", "resim"])
+    ap.add_argument("--workload", default="hit", choices=["hit", "channel", "resim", "adjoint"])
+    ap.add_argument("--adj-steps", type=int, default=50)
+    ap.add_argument("--adj-ckpt", type=int, default=10)
+    ap.add_argument("--adj-dirs", type=int, default=32)
+    ap.add_argument("--adj-eps", type=float, default=1e-5)
     ap.add_argument("--autotune", action="store_true", help="resim: autotune the batched stage kernels first")
     args = ap.parse_args()
     if args.workload == "resim" and args.impl != "reference":
         return run_resim(args)
+    if args.workload == "adjoint" and args.impl != "reference":
+        return run_adjoint(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -204,14 +204,23 @@ class Session:
         """Run nsteps steps keeping a checkpoint every ckpt_every steps (ns_adj_forward)."""
         self._check(self.lib.ns_adj_forward(self.h, int(nsteps), int(ckpt_every)))
 
-    def adj_backward(self, dJ_du, dJ_dv, dJ_dw, history=False):
+    def adj_backward(self, dJ_du, dJ_dv, dJ_dw, history=False, out=None):
         """Gradient of J(u(T)) with respect to the initial u, v, w (ns_adj_backward).
 
         Returns {"u", "v", "w"} (and "hx", "hy", "hz" with history=True) in the
-        reference shapes, zero on the entries that are periodic copies."""
+        reference shapes, zero on the entries that are periodic copies.  `out`
+        may hold preallocated Fortran-ordered arrays "u", "v", "w" (e.g. in
+        pinned host memory) that receive the gradient."""
         sh = self.shapes
         seeds = [_f(dJ_du, sh["u"]), _f(dJ_dv, sh["v"]), _f(dJ_dw, sh["w"])]
-        out = {k: np.zeros(sh[k], order="F") for k in ("u", "v", "w")}
+        if out is None:
+            out = {k: np.zeros(sh[k], order="F") for k in ("u", "v", "w")}
+        else:
+            for k in ("u", "v", "w"):
+                a = out[k]
+                if a.shape != sh[k] or a.dtype != np.float64 or not a.flags.f_contiguous:
+                    raise NSError(6, f"out[{k!r}] must be a Fortran-ordered float64 array of shape {sh[k]}")
+            out = dict(out)
         hist = [np.zeros(sh[k], order="F") for k in ("u", "v", "w")] if history else [None] * 3
         self._check(self.lib.ns_adj_backward(self.h, *[_ptr(a) for a in seeds], _ptr(out["u"]), _ptr(out["v"]),
                                              _ptr(out["w"]), _ptr(hist[0]), _ptr(hist[1]), _ptr(hist[2])))

@@ -56,13 +56,13 @@ struct AdjArgs {
   double ax, ay, az;    // -1/(4 dx) etc.
   double ax2, ay2, az2; // 2 ax etc.
   double l0, lx, ly, lz;  // Laplacian part: l0 X + lx (X[i-1] + X[i+1]) + ...
+  int kc;               // z planes per CTA (set by the launcher)
 };
 
 namespace {
 
 constexpr int AX = 32;       // output x-slots per row
 constexpr int AY = 8;        // output rows
-constexpr int AKC = 16;      // z planes per CTA
 constexpr int IW = AX + 2;   // staged input row: x in [i0-1, i0+AX]
 constexpr int IH = AY + 2;   // staged input rows: y in [j0-1, j0+AY]
 constexpr int PW = AX + 1;   // product positions per row: x in [i0, i0+AX]
@@ -182,8 +182,8 @@ __global__ void __launch_bounds__(32 * PH, 3) adj_predict_kernel(AdjArgs a) {
   const int lane = threadIdx.x, wy = threadIdx.y;  // position (lane, wy)
   const int i0 = 1 + AX * blockIdx.x;
   const int j0 = 1 + AY * blockIdx.y;
-  const int k0 = 1 + AKC * blockIdx.z;
-  const int k1 = min(k0 + AKC, L.nz + 1);
+  const int k0 = 1 + a.kc * blockIdx.z;
+  const int k1 = min(k0 + a.kc, L.nz + 1);
   // warm-up: planes k0-1, k0 and the z-face products at k0
   adj_load_plane<HAS_NEXT>(S, a, c, i0, j0, k0 - 1);
   adj_load_plane<HAS_NEXT>(S, a, c, i0, j0, k0);
@@ -224,13 +224,38 @@ __global__ void __launch_bounds__(32 * PH, 3) adj_predict_kernel(AdjArgs a) {
   }
 }
 
+// z-chunk length: the number of chunks c that minimises the time of the
+// grid in waves of resident CTAs, ceil(cols c / slots) * (ceil(nz / c) + 2),
+// where the 2 stands for a chunk's warm-up (two planes loaded, one plane of
+// products).  At 128^3 this gives 7 chunks of 19 planes (448 CTAs on 456
+// slots) instead of 8 chunks (512 CTAs, 1.12 waves).
+static int adj_chunk(int cols, int nz, int slots) {
+  int best = nz, bc = 1;
+  double best_t = 1e300;
+  for (int c = 1; c <= nz; ++c) {
+    const int kc = (nz + c - 1) / c;
+    const int cc = (nz + kc - 1) / kc;  // chunks actually launched
+    const double waves = std::ceil((double)cols * cc / slots);
+    const double t = waves * (kc + 2);
+    if (t < best_t - 1e-9) { best_t = t; best = kc; bc = cc; }
+  }
+  (void)bc;
+  return best;
+}
+
 template <bool LAPG, bool HAS_NEXT>
-static cudaError_t launch_adj_t(const AdjArgs& a, cudaStream_t st) {
+static cudaError_t launch_adj_t(AdjArgs a, cudaStream_t st) {
   auto kern = adj_predict_kernel<LAPG, HAS_NEXT>;
   const size_t sm = sizeof(AdjSmem);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  dim3 grid((a.L.nx + AX - 1) / AX, (a.L.ny + AY - 1) / AY, (a.L.nz + AKC - 1) / AKC);
+  int dev = 0, nsm = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * PH, sm)) != cudaSuccess) return e;
+  const int gx = (a.L.nx + AX - 1) / AX, gy = (a.L.ny + AY - 1) / AY;
+  a.kc = adj_chunk(gx * gy, a.L.nz, std::max(1, per_sm) * std::max(1, nsm));
+  dim3 grid(gx, gy, (a.L.nz + a.kc - 1) / a.kc);
   kern<<<grid, dim3(32, PH), sm, st>>>(a);
   return cudaGetLastError();
 }
@@ -262,6 +287,49 @@ __global__ void __launch_bounds__(256) periodic_fill_kernel(Layout L, double* f0
     x[0] = x[(long long)n * st];
     x[(long long)(n + 1) * st] = x[st];
   }
+}
+
+// Transpose of the periodic images along AXIS (FOLD): X[n] += X[0],
+// X[1] += X[n+1], then both ghosts zeroed; or (!FOLD) the ghosts zeroed
+// only.  Three passes x, y, z carry a corner entry to its owner in hops.
+template <int AXIS, bool FOLD>
+__global__ void __launch_bounds__(256) periodic_fold_kernel(Layout L, double* f0, double* f1, double* f2) {
+  const int n1 = (AXIS == 0) ? L.ny + 2 : L.nx + 2;
+  const int n2 = (AXIS == 2) ? L.ny + 2 : L.nz + 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n1 * n2) return;
+  const int s1 = t % n1, s2 = t / n1;
+  long long base, st;
+  int n;
+  if (AXIS == 0) { base = L.at(0, s1, s2); st = 1; n = L.nx; }
+  else if (AXIS == 1) { base = L.at(s1, 0, s2); st = L.sy; n = L.ny; }
+  else { base = L.at(s1, s2, 0); st = L.sz; n = L.nz; }
+  double* f[3] = {f0, f1, f2};
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    double* x = f[q] + base;
+    double* hi = x + (long long)(n + 1) * st;
+    if (FOLD) {
+      x[(long long)n * st] += x[0];
+      x[st] += *hi;
+    }
+    x[0] = 0.0;
+    *hi = 0.0;
+  }
+}
+
+cudaError_t launch_periodic_fold(const Layout& L, double* f0, double* f1, double* f2, bool fold, cudaStream_t st) {
+  for (int a = 0; a < 3; ++a) {
+    const int n = plane_count(L, a);
+    const dim3 grid((n + 255) / 256);
+    if (a == 0) fold ? periodic_fold_kernel<0, true><<<grid, 256, 0, st>>>(L, f0, f1, f2)
+                     : periodic_fold_kernel<0, false><<<grid, 256, 0, st>>>(L, f0, f1, f2);
+    if (a == 1) fold ? periodic_fold_kernel<1, true><<<grid, 256, 0, st>>>(L, f0, f1, f2)
+                     : periodic_fold_kernel<1, false><<<grid, 256, 0, st>>>(L, f0, f1, f2);
+    if (a == 2) fold ? periodic_fold_kernel<2, true><<<grid, 256, 0, st>>>(L, f0, f1, f2)
+                     : periodic_fold_kernel<2, false><<<grid, 256, 0, st>>>(L, f0, f1, f2);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_periodic_fill(const Layout& L, double* f0, double* f1, double* f2, cudaStream_t st) {
@@ -355,28 +423,10 @@ int adj_ensure(ns_handle* h) {
   return NS_OK;
 }
 
-// Reference extent of field f (0 u, 1 v, 2 w) along axis a, and the 0-based
-// reference index of the independent slot that reference index r copies.
+// Reference extent of field f (0 u, 1 v, 2 w) along axis a.
 inline int ref_ext(const ns_config& c, int f, int a) {
   const int n = a == 0 ? c.nx : (a == 1 ? c.ny : c.nz);
   return f == a ? n + 1 : n + 2;
-}
-inline int ref_owner(int r, int n, bool face) { return face ? r % n : ((r - 1 + n) % n) + 1; }
-
-// Adjoint seed: every entry added into the independent value it aliases,
-// zero elsewhere (the transpose of the periodic copies).
-void fold_periodic(const ns_config& c, int f, const double* in, std::vector<double>& out) {
-  const int ex = ref_ext(c, f, 0), ey = ref_ext(c, f, 1), ez = ref_ext(c, f, 2);
-  out.assign((size_t)ex * ey * ez, 0.0);
-  for (int k = 0; k < ez; ++k) {
-    const int kk = ref_owner(k, c.nz, f == 2);
-    for (int j = 0; j < ey; ++j) {
-      const int jj = ref_owner(j, c.ny, f == 1);
-      const size_t row_in = (size_t)ex * (j + (size_t)ey * k);
-      const size_t row_out = (size_t)ex * (jj + (size_t)ey * kk);
-      for (int i = 0; i < ex; ++i) out[row_out + ref_owner(i, c.nx, f == 0)] += in[row_in + i];
-    }
-  }
 }
 
 // Zero every entry that is a periodic copy (gradients are with respect to
@@ -555,13 +605,15 @@ int ns_adj_backward(ns_handle* h, const double* dJ_du, const double* dJ_dv, cons
   if (!A || !A->ready) return api_fail(h, NS_ERR_ARG, "adjoint: call ns_adj_forward first");
   const ns_config& c = h->cfg;
   int s;
-  // seed: the folded dJ/du(T), with periodic images
+  // seed: dJ/du(T) with every periodic copy folded into its owner, then
+  // the images refilled
   const double* seeds[3] = {dJ_du, dJ_dv, dJ_dw};
-  std::vector<std::vector<double>> folded(3);
   for (int f = 0; f < 3; ++f) {
-    fold_periodic(c, f, seeds[f], folded[f]);
-    ADJ_CUDA(h, api_h2d_field(h, A->lam[f], folded[f].data(), f));
+    ADJ_CUDA(h, cudaMemsetAsync(A->lam[f], 0, h->L.fsize * sizeof(double), h->stream));
+    ADJ_CUDA(h, api_h2d_field(h, A->lam[f], seeds[f], f));
   }
+  ADJ_CUDA(h, launch_periodic_fold(h->L, A->lam[0], A->lam[1], A->lam[2], true, h->stream));
+  api_mark(h, "adj_fold", 3);
   ADJ_CUDA(h, launch_periodic_fill(h->L, A->lam[0], A->lam[1], A->lam[2], h->stream));
   api_mark(h, "adj_fill", 3);
   A->cur = 0;
@@ -587,7 +639,10 @@ int ns_adj_backward(ns_handle* h, const double* dJ_du, const double* dJ_dv, cons
       if ((s = adj_backward_step(h, A, fwd, A->seg_first[n - s0] != 0, has_next))) return s;
     }
   }
-  // gradients with respect to the independent values of u0, v0, w0
+  // gradients with respect to the independent values of u0, v0, w0 (the
+  // periodic copies zeroed)
+  ADJ_CUDA(h, launch_periodic_fold(h->L, A->lam[0], A->lam[1], A->lam[2], false, h->stream));
+  api_mark(h, "adj_zero", 3);
   double* gr[3] = {grad_u, grad_v, grad_w};
   for (int f = 0; f < 3; ++f) ADJ_CUDA(h, api_d2h_field(h, gr[f], A->lam[f], f));
   // history input of step 0: cP ls of step 0 (zero after an Euler start)
@@ -596,7 +651,6 @@ int ns_adj_backward(ns_handle* h, const double* dJ_du, const double* dJ_dv, cons
   for (int f = 0; f < 3; ++f)
     if (gh[f] && hist_used) ADJ_CUDA(h, api_d2h_field(h, gh[f], A->ls[1 - A->cur][f], f));
   ADJ_CUDA(h, cudaStreamSynchronize(h->stream));
-  for (int f = 0; f < 3; ++f) zero_copies(c, f, gr[f]);
   for (int f = 0; f < 3; ++f) {
     if (!gh[f]) continue;
     const size_t n = (size_t)ref_ext(c, f, 0) * ref_ext(c, f, 1) * ref_ext(c, f, 2);
