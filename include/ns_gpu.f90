@@ -31,6 +31,19 @@ module ns_gpu
     integer(c_int) :: euler_start_pending, reserved
   end type ns_diag
 
+  ! Batched tier (re_simulation_sub_tstep_interBC_combine.f90:415-811 for many sub-blocks at once).
+  type, bind(C) :: ns_subdomain
+    integer(c_int) :: x0, y0, z0          ! 1-based origin in the parent (idx_xu = x0 + (0..nx))
+    integer(c_int) :: nx, ny, nz
+    integer(c_int) :: sub_tstep, reserved
+  end type ns_subdomain
+
+  type, bind(C) :: ns_batch_config
+    integer(c_int) :: scheme, bc, pbc, restart, n_slots, mode, use_graph
+    real(c_double) :: nu, dt0, dx, dy, dz
+    integer(c_int) :: grid(16), reserved(8)
+  end type ns_batch_config
+
   interface
     integer(c_int) function ns_config_default(cfg, nx, ny, nz) bind(C, name="ns_config_default")
       import :: c_int, ns_config
@@ -106,6 +119,73 @@ module ns_gpu
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: h
       real(c_double), intent(inout) :: us(*), vs(*), ws(*)
+    end function
+
+    ! --- batched re-simulation --------------------------------------------------
+    subroutine ns_batch_config_default(cfg) bind(C, name="ns_batch_config_default")
+      import :: ns_batch_config
+      type(ns_batch_config), intent(out) :: cfg
+    end subroutine
+
+    integer(c_int) function ns_batch_create(cfg, subs, n, b) bind(C, name="ns_batch_create")
+      import :: c_int, c_ptr, ns_batch_config, ns_subdomain
+      type(ns_batch_config), intent(in) :: cfg
+      type(ns_subdomain), intent(in) :: subs(*)
+      integer(c_int), value :: n
+      type(c_ptr), intent(out) :: b
+    end function
+
+    integer(c_int) function ns_batch_destroy(b) bind(C, name="ns_batch_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b
+    end function
+
+    integer(c_int) function ns_batch_init_from_parent(b, parent) bind(C, name="ns_batch_init_from_parent")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b, parent
+    end function
+
+    integer(c_int) function ns_batch_capture(b, parent, slot, t) bind(C, name="ns_batch_capture")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b, parent
+      integer(c_int), value :: slot
+      real(c_double), value :: t
+    end function
+
+    integer(c_int) function ns_batch_advance(b, t0) bind(C, name="ns_batch_advance")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      real(c_double), value :: t0
+    end function
+
+    integer(c_int) function ns_batch_get_state(b, i, u, v, w, p, rx, ry, rz) bind(C, name="ns_batch_get_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      integer(c_int), value :: i                   ! 0-based subdomain index
+      real(c_double), intent(out), optional :: u(*), v(*), w(*), p(*), rx(*), ry(*), rz(*)
+    end function
+
+    integer(c_int) function ns_batch_max_div(b, i, max_div) bind(C, name="ns_batch_max_div")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      integer(c_int), value :: i
+      real(c_double), intent(out) :: max_div
+    end function
+
+    ! --- discrete adjoint (no counterpart in the reference) -----------------------
+    integer(c_int) function ns_adj_forward(h, nsteps, ckpt_every) bind(C, name="ns_adj_forward")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: nsteps, ckpt_every
+    end function
+
+    integer(c_int) function ns_adj_backward(h, gu, gv, gw, du0, dv0, dw0, dhx, dhy, dhz) &
+        bind(C, name="ns_adj_backward")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: gu(*), gv(*), gw(*)          ! dJ/du(T), dJ/dv(T), dJ/dw(T)
+      real(c_double), intent(out) :: du0(*), dv0(*), dw0(*)      ! dJ/du(0) ...
+      real(c_double), intent(out), optional :: dhx(*), dhy(*), dhz(*)
     end function
   end interface
 end module ns_gpu
