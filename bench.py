@@ -637,6 +637,19 @@ def run_ours(args):
                                       P(hout_h[0]), P(hout_h[1]), P(hout_h[2])))
         torch.cuda.synchronize()
         e2e_sec = time.perf_counter() - t0
+        # one more round, phase by phase (each phase ends synchronised)
+        tp = [time.perf_counter()]
+        s._check(lib.ns_set_state(s.h, P(hin["u"]), P(hin["v"]), P(hin["w"]), P(hin["p"]),
+                                  P(hhist[0]), P(hhist[1]), P(hhist[2])))
+        tp.append(time.perf_counter())
+        s._check(lib.ns_step(s.h, 1))
+        s._check(lib.ns_synchronize(s.h))
+        tp.append(time.perf_counter())
+        s._check(lib.ns_get_state(s.h, P(hout["u"]), P(hout["v"]), P(hout["w"]), P(hout["p"]),
+                                  P(hout_h[0]), P(hout_h[1]), P(hout_h[2])))
+        tp.append(time.perf_counter())
+        e2e_phases = {"set_state_ms": 1e3 * (tp[1] - tp[0]), "step_ms": 1e3 * (tp[2] - tp[1]),
+                      "get_state_ms": 1e3 * (tp[3] - tp[2])}
         barrier()
         e2e_value = world * ncell * e2e_steps / e2e_sec
 
@@ -665,7 +678,8 @@ def run_ours(args):
                  if args.workload == "hit" else "synthetic (laminar profile + seeded divergence-free perturbation)"),
         "config": W["config"] | {"parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps, "path": "ns_set_state (pinned host) + ns_step + ns_get_state (pinned host)"},
+                "steps": e2e_steps, "path": "ns_set_state (pinned host) + ns_step + ns_get_state (pinned host)",
+                "phases": e2e_phases},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,

@@ -198,29 +198,158 @@ inline int ext_of(const ns_config& c, int field, int axis) {
   return (field == axis) ? n + 1 : n + 2;
 }
 
+// Host <-> device field transfers.  A reference-shaped array moves as ONE
+// flat copy between host memory and a device staging buffer (full link
+// bandwidth; a pitched 3D copy issues one DMA per 2 KB row), and a kernel
+// scatters it into, or gathers it from, the padded slot layout.  On the way
+// out, entries outside [lo, hi] per axis (0-based reference indices) can be
+// written as zero (the history outside its interior ranges).
+struct PackArgs {
+  Layout L;
+  double* field;
+  double* stage;
+  int ex, ey, ez;   // reference extents
+  int ox, oy, oz;   // slot of reference index 0 per axis
+  int to_field;     // 1: stage -> field, 0: field -> stage
+  int lo[3], hi[3]; // kept range on the way out (others zero)
+};
+
+__global__ void __launch_bounds__(256) field_pack_kernel(PackArgs a) {
+  const long long n = (long long)a.ex * a.ey * a.ez;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % a.ex);
+    const long long r = t / a.ex;
+    const int j = (int)(r % a.ey);
+    const int k = (int)(r / a.ey);
+    const long long g = a.L.at(a.ox + i, a.oy + j, a.oz + k);
+    if (a.to_field) {
+      a.field[g] = a.stage[t];
+    } else {
+      const bool keep = i >= a.lo[0] && i <= a.hi[0] && j >= a.lo[1] && j <= a.hi[1] && k >= a.lo[2] && k <= a.hi[2];
+      a.stage[t] = keep ? a.field[g] : 0.0;
+    }
+  }
+}
+
+cudaError_t ensure_stage(ns_handle* h) {
+  if (h->stage) return cudaSuccess;
+  const size_t n = (size_t)(h->cfg.nx + 2) * (h->cfg.ny + 2) * (h->cfg.nz + 2);
+  return cudaMalloc(&h->stage, n * sizeof(double));
+}
+
+// The second staging buffer, the copy stream and its events (multi-field transfers).
+cudaError_t ensure_xfer(ns_handle* h) {
+  cudaError_t e = ensure_stage(h);
+  if (e != cudaSuccess || h->stage2) return e;
+  const size_t n = (size_t)(h->cfg.nx + 2) * (h->cfg.ny + 2) * (h->cfg.nz + 2);
+  if ((e = cudaMalloc(&h->stage2, n * sizeof(double))) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  for (int b = 0; b < 2; ++b) {
+    if ((e = cudaEventCreateWithFlags(&h->ev_full[b], cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t pack_launch(ns_handle* h, double* field, double* stage, int f, bool to_field, const int* lo = nullptr,
+                        const int* hi = nullptr) {
+  const ns_config& c = h->cfg;
+  PackArgs a{};
+  a.L = h->L;
+  a.field = field;
+  a.stage = stage;
+  a.ex = ext_of(c, f, 0); a.ey = ext_of(c, f, 1); a.ez = ext_of(c, f, 2);
+  a.ox = 1 + slot_off(f, 0); a.oy = 1 + slot_off(f, 1); a.oz = 1 + slot_off(f, 2);
+  a.to_field = to_field ? 1 : 0;
+  const int ext[3] = {a.ex, a.ey, a.ez};
+  for (int q = 0; q < 3; ++q) {
+    a.lo[q] = lo ? lo[q] : 0;
+    a.hi[q] = hi ? hi[q] : ext[q] - 1;
+  }
+  const long long n = (long long)a.ex * a.ey * a.ez;
+  const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  field_pack_kernel<<<grid, 256, 0, h->stream>>>(a);
+  return cudaGetLastError();
+}
+
+inline size_t field_bytes(const ns_config& c, int f) {
+  return sizeof(double) * ext_of(c, f, 0) * ext_of(c, f, 1) * ext_of(c, f, 2);
+}
+
+// n fields in: copies on the copy stream, scatters on the handle's stream,
+// two staging buffers in turn so the copy of one field overlaps the scatter
+// of the previous one.
+cudaError_t h2d_fields(ns_handle* h, int n, double* const* dst, const double* const* src, const int* fid) {
+  cudaError_t e = ensure_xfer(h);
+  if (e != cudaSuccess) return e;
+  double* buf[2] = {h->stage, h->stage2};
+  for (int b = 0; b < 2; ++b)
+    if ((e = cudaEventRecord(h->ev_free[b], h->stream)) != cudaSuccess) return e;
+  for (int q = 0; q < n; ++q) {
+    const int b = q & 1;
+    if ((e = cudaStreamWaitEvent(h->xfer, h->ev_free[b], 0)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(buf[b], src[q], field_bytes(h->cfg, fid[q]), cudaMemcpyHostToDevice, h->xfer)) !=
+        cudaSuccess)
+      return e;
+    if ((e = cudaEventRecord(h->ev_full[b], h->xfer)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(h->stream, h->ev_full[b], 0)) != cudaSuccess) return e;
+    if ((e = pack_launch(h, dst[q], buf[b], fid[q], true)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(h->ev_free[b], h->stream)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// n fields out: gathers on the handle's stream, copies on the copy stream;
+// returns after the last copy has landed.  zero_hist[q]: zero the entries
+// outside the history's interior ranges.
+cudaError_t d2h_fields(ns_handle* h, int n, double* const* dst, const double* const* src, const int* fid,
+                       const bool* zero_hist) {
+  cudaError_t e = ensure_xfer(h);
+  if (e != cudaSuccess) return e;
+  const ns_config& c = h->cfg;
+  double* buf[2] = {h->stage, h->stage2};
+  for (int b = 0; b < 2; ++b)
+    if ((e = cudaEventRecord(h->ev_free[b], h->xfer)) != cudaSuccess) return e;
+  for (int q = 0; q < n; ++q) {
+    const int b = q & 1, f = fid[q];
+    if ((e = cudaStreamWaitEvent(h->stream, h->ev_free[b], 0)) != cudaSuccess) return e;
+    int lo[3], hi[3];
+    for (int ax = 0; ax < 3; ++ax) {  // the history's interior ranges (0-based reference indices)
+      const int na = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
+      if (ax == f) { lo[ax] = c.bc[ax] == 1 ? 0 : 1; hi[ax] = na - 1; }
+      else { lo[ax] = 1; hi[ax] = na; }
+    }
+    const bool z = zero_hist && zero_hist[q];
+    if ((e = pack_launch(h, const_cast<double*>(src[q]), buf[b], f, false, z ? lo : nullptr, z ? hi : nullptr)) !=
+        cudaSuccess)
+      return e;
+    if ((e = cudaEventRecord(h->ev_full[b], h->stream)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(h->xfer, h->ev_full[b], 0)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(dst[q], buf[b], field_bytes(c, f), cudaMemcpyDeviceToHost, h->xfer)) != cudaSuccess)
+      return e;
+    if ((e = cudaEventRecord(h->ev_free[b], h->xfer)) != cudaSuccess) return e;
+  }
+  return cudaStreamSynchronize(h->xfer);
+}
+
 // Copy a Fortran array (reference shape) into the padded device field.
 cudaError_t h2d_field(ns_handle* h, double* dst, const double* src, int field) {
   const ns_config& c = h->cfg;
-  const int ex = ext_of(c, field, 0), ey = ext_of(c, field, 1), ez = ext_of(c, field, 2);
-  cudaMemcpy3DParms prm{};
-  prm.srcPtr = make_cudaPitchedPtr((void*)src, ex * sizeof(double), ex, ey);
-  prm.dstPtr = make_cudaPitchedPtr((void*)(dst + h->L.off), h->L.px * sizeof(double), h->L.px, c.ny + 2);
-  prm.dstPos = make_cudaPos((1 + slot_off(field, 0)) * sizeof(double), 1 + slot_off(field, 1), 1 + slot_off(field, 2));
-  prm.extent = make_cudaExtent(ex * sizeof(double), ey, ez);
-  prm.kind = cudaMemcpyHostToDevice;
-  return cudaMemcpy3DAsync(&prm, h->stream);
+  const size_t bytes = sizeof(double) * ext_of(c, field, 0) * ext_of(c, field, 1) * ext_of(c, field, 2);
+  cudaError_t e = ensure_stage(h);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(h->stage, src, bytes, cudaMemcpyHostToDevice, h->stream)) != cudaSuccess) return e;
+  return pack_launch(h, dst, h->stage, field, true);
 }
 
 cudaError_t d2h_field(ns_handle* h, double* dst, const double* src, int field) {
   const ns_config& c = h->cfg;
-  const int ex = ext_of(c, field, 0), ey = ext_of(c, field, 1), ez = ext_of(c, field, 2);
-  cudaMemcpy3DParms prm{};
-  prm.srcPtr = make_cudaPitchedPtr((void*)(src + h->L.off), h->L.px * sizeof(double), h->L.px, c.ny + 2);
-  prm.srcPos = make_cudaPos((1 + slot_off(field, 0)) * sizeof(double), 1 + slot_off(field, 1), 1 + slot_off(field, 2));
-  prm.dstPtr = make_cudaPitchedPtr((void*)dst, ex * sizeof(double), ex, ey);
-  prm.extent = make_cudaExtent(ex * sizeof(double), ey, ez);
-  prm.kind = cudaMemcpyDeviceToHost;
-  return cudaMemcpy3DAsync(&prm, h->stream);
+  const size_t bytes = sizeof(double) * ext_of(c, field, 0) * ext_of(c, field, 1) * ext_of(c, field, 2);
+  cudaError_t e = ensure_stage(h);
+  if (e != cudaSuccess) return e;
+  if ((e = pack_launch(h, const_cast<double*>(src), h->stage, field, false)) != cudaSuccess) return e;
+  return cudaMemcpyAsync(dst, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream);
 }
 
 // Plane size of face planes for an axis (full box extent of the two other axes).
@@ -616,6 +745,13 @@ void free_all(ns_handle* h) {
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (h->spec) cudaFree(h->spec);
+  if (h->stage) cudaFree(h->stage);
+  if (h->stage2) cudaFree(h->stage2);
+  if (h->xfer) cudaStreamDestroy(h->xfer);
+  for (int b = 0; b < 2; ++b) {
+    if (h->ev_full[b]) cudaEventDestroy(h->ev_full[b]);
+    if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
+  }
   if (h->tw) cudaFree(h->tw);
   if (h->diag_bits) cudaFree(h->diag_bits);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -740,18 +876,14 @@ int ns_synchronize(ns_handle* h) {
 int ns_set_state(ns_handle* h, const double* u, const double* v, const double* w, const double* p, const double* hx,
                  const double* hy, const double* hz) {
   if (!h || !u || !v || !w || !p) return fail(h, NS_ERR_ARG, "u, v, w, p are required");
-  NS_CUDA(h, h2d_field(h, h->u, u, 0));
-  NS_CUDA(h, h2d_field(h, h->v, v, 1));
-  NS_CUDA(h, h2d_field(h, h->w, w, 2));
-  NS_CUDA(h, h2d_field(h, h->p, p, 3));
+  const bool hist = hx && hy && hz;
+  double* dst[7] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz};
+  const double* src[7] = {u, v, w, p, hx, hy, hz};
+  const int fid[7] = {0, 1, 2, 3, 0, 1, 2};
+  NS_CUDA(h, h2d_fields(h, hist ? 7 : 4, dst, src, fid));
   // The extra face slot 0 of a periodic axis mirrors face n.
   NS_CUDA(h, launch_extra_slots(h->L, h->u, h->v, h->w, h->cfg.bc, h->stream));
-  const bool hist = hx && hy && hz;
-  if (hist) {
-    NS_CUDA(h, h2d_field(h, h->hx, hx, 0));
-    NS_CUDA(h, h2d_field(h, h->hy, hy, 1));
-    NS_CUDA(h, h2d_field(h, h->hz, hz, 2));
-  } else {
+  if (!hist) {
     NS_CUDA(h, cudaMemsetAsync(h->hx, 0, h->L.fsize * sizeof(double), h->stream));
     NS_CUDA(h, cudaMemsetAsync(h->hy, 0, h->L.fsize * sizeof(double), h->stream));
     NS_CUDA(h, cudaMemsetAsync(h->hz, 0, h->L.fsize * sizeof(double), h->stream));
@@ -764,39 +896,22 @@ int ns_set_state(ns_handle* h, const double* u, const double* v, const double* w
 
 int ns_get_state(ns_handle* h, double* u, double* v, double* w, double* p, double* hx, double* hy, double* hz) {
   if (!h) return NS_ERR_ARG;
-  if (u) NS_CUDA(h, d2h_field(h, u, h->u, 0));
-  if (v) NS_CUDA(h, d2h_field(h, v, h->v, 1));
-  if (w) NS_CUDA(h, d2h_field(h, w, h->w, 2));
-  if (p) NS_CUDA(h, d2h_field(h, p, h->p, 3));
-  if (hx) NS_CUDA(h, d2h_field(h, hx, h->hx, 0));
-  if (hy) NS_CUDA(h, d2h_field(h, hy, h->hy, 1));
-  if (hz) NS_CUDA(h, d2h_field(h, hz, h->hz, 2));
-  NS_CUDA(h, cudaStreamSynchronize(h->stream));
-  // History outside the interior ranges is returned as zero.
-  const ns_config& c = h->cfg;
-  double* hs[3] = {hx, hy, hz};
-  for (int f = 0; f < 3; ++f) {
-    double* a = hs[f];
-    if (!a) continue;
-    const int ex = ext_of(c, f, 0), ey = ext_of(c, f, 1), ez = ext_of(c, f, 2);
-    // interior range (0-based) per axis: the field's own axis 1..n-1 or 0..n-1, others 1..n
-    int lo[3], hi[3];
-    for (int ax = 0; ax < 3; ++ax) {
-      const int n = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
-      if (ax == f) { lo[ax] = c.bc[ax] == 1 ? 0 : 1; hi[ax] = n - 1; }
-      else { lo[ax] = 1; hi[ax] = n; }
-    }
-    for (int k = 0; k < ez; ++k)
-      for (int j = 0; j < ey; ++j) {
-        double* row = a + (size_t)ex * (j + (size_t)ey * k);
-        if (k < lo[2] || k > hi[2] || j < lo[1] || j > hi[1]) {
-          std::memset(row, 0, sizeof(double) * ex);
-          continue;
-        }
-        for (int i = 0; i < lo[0]; ++i) row[i] = 0.0;
-        for (int i = hi[0] + 1; i < ex; ++i) row[i] = 0.0;
-      }
+  double* const all_dst[7] = {u, v, w, p, hx, hy, hz};
+  const double* all_src[7] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz};
+  double* dst[7];
+  const double* src[7];
+  int fid[7];
+  bool zero[7];
+  int n = 0;
+  for (int q = 0; q < 7; ++q) {
+    if (!all_dst[q]) continue;
+    dst[n] = all_dst[q];
+    src[n] = all_src[q];
+    fid[n] = q < 4 ? q : q - 4;
+    zero[n] = q >= 4;  // history outside the interior ranges is returned as zero
+    ++n;
   }
+  NS_CUDA(h, d2h_fields(h, n, dst, src, fid, zero));
   return NS_OK;
 }
 

@@ -26,6 +26,10 @@ struct ns_handle {
   double *us = nullptr, *vs = nullptr, *ws = nullptr, *dp = nullptr;
   double *us2 = nullptr, *vs2 = nullptr, *ws2 = nullptr;  // ADI ping-pong buffers
   double2* spec = nullptr;
+  double* stage = nullptr;   // host<->device staging of one reference-shaped field
+  double* stage2 = nullptr;  // second staging buffer (multi-field transfers)
+  cudaStream_t xfer = nullptr;  // copy stream of the multi-field transfers
+  cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   double* inv_lam = nullptr;
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
   ns::FftPlan plan{};
