@@ -63,6 +63,15 @@ ALG_DOUBLES = {
     "tri_y_solve": 2.0,   # read + write half spectrum (line solves along the wall axis)
 }
 
+# FP64 instructions per cell of each kernel (thread-level, adds and multiplies
+# issued as DFMA), from ncu's sm__sass_thread_inst_executed_op_dfma_pred_on.sum
+# of this build's kernels at 256^3 divided by the cells of one launch.
+FP64_PER_CELL = {
+    "predict": 62.7, "adi_x": 9.5, "adi_y": 9.5, "adi_z": 9.5, "fft_x_fwd": 18.8, "fft_y_fwd": 11.2,
+    "fft_z_solve": 23.4, "fft_y_inv": 11.2, "fft_x_inv": 12.7, "correct": 7.2,
+}
+FP64_LANES_PER_CLK_SM = 2  # DFMA issue rate of this part (ncu ..._op_dfma_pred_on.sum.peak_sustained)
+
 # DRAM bytes per launch at 256^3 (dram__bytes_read.sum + dram__bytes_write.sum)
 # from one ncu capture of each kernel of this build's step.
 NCU_TRAFFIC_256 = {
@@ -384,7 +393,7 @@ def run_resim(args):
         for b in batches.values():
             b.close()
     if rank != 0:
-        return 0
+        return None
     line = {
         "metric": "FP64 subdomain cell-steps/s, batched re-simulation of 64 sub-blocks (128^3 periodic parent)",
         "value": out[0]["value"], "unit": UNIT, "n_gpus": world, "steps": T - 1, "warmup": 1,
@@ -404,8 +413,7 @@ def run_resim(args):
         "e2e": {"value": work / job_sec, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "path": "whole job: parent steps + snapshot captures + both batches (mode 0 and 1)"},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def _slots(a, which, n):
@@ -525,7 +533,7 @@ def run_adjoint(args):
             errs.append(abs(fd - ad) / abs(ad))
         fd_sec = time.perf_counter() - t_fd
     if rank != 0:
-        return 0
+        return None
     line = {
         "metric": "FP64 adjoint cell-steps/s (dJ/du0 over 50 AB2-CN steps of a 128^3 periodic box, checkpoint every 10)",
         "value": ncell * T / (bwd_ms * T / 1e3), "unit": UNIT, "n_gpus": world, "steps": T, "warmup": 1,
@@ -548,8 +556,7 @@ def run_adjoint(args):
                 "d2h_bytes_per_step": 3 * 8 * (n + 1) * (n + 2) ** 2 / T,
                 "path": "ns_adj_forward + ns_adj_backward (pinned host seed in, pinned host gradient out)"},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def run_ours(args):
@@ -670,6 +677,18 @@ def run_ours(args):
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
     traffic = NCU_TRAFFIC_256.get(dname) if (n == 256 and args.workload == "hit") else None
     total_prof = sum(v[0] for v in prof.values())
+    # FP64 roof: DFMA lanes per clock x SMs x the SM clock sampled in the timed region
+    clk_s = clk.summary()
+    sm_mhz = clk_s.get("sm_mhz") or 2070.0
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    fp64_peak = FP64_LANES_PER_CLK_SM * nsm * sm_mhz * 1e6 / 1e9  # G FP64 inst/s
+    fp64_roof = None
+    if args.workload == "hit":
+        dom_fp = FP64_PER_CELL.get(dname, 0.0) * ncell / (per_launch_ms / 1e3) / 1e9
+        step_fp = sum(FP64_PER_CELL.get(k, 0.0) * ncell * v[1] / 2 for k, v in prof.items()) / (ms_per_step / 1e3) / 1e9
+        fp64_roof = {"bound": "fp64", "kernel": dname, "achieved": dom_fp, "peak": fp64_peak, "unit": "G FP64 inst/s",
+                     "frac": dom_fp / fp64_peak, "step_achieved": step_fp, "step_frac": step_fp / fp64_peak,
+                     "peak_source": f"{FP64_LANES_PER_CLK_SM} DFMA lanes/clk/SM x {nsm} SMs x {sm_mhz:.0f} MHz"}
     line = {
         "metric": W["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -684,12 +703,33 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
                      "alg_bytes_per_launch": alg_bytes, "ms_per_launch": per_launch_ms,
-                     "note": "the step is FP64-pipe bound on this part (measured ~0.6 T DFMA/s); see fp64"},
+                     "note": "the step is bound by the FP64 pipe, not HBM, on this part: see the fp64 object"},
+        "fp64": fp64_roof,
         "kernel_ms_per_step": {k: v[0] / 2 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "kernel_share": {k: v[0] / total_prof for k, v in prof.items()},
-        "clocks": clk.summary(),
+        "clocks": clk_s,
         "diag": {"max_div": d["max_div"], "probe": d["probe"]},
     }
+    if args.extras and world == 1 and args.workload == "hit":
+        # the other two targets of the step, measured in the same run
+        try:
+            a = argparse.Namespace(**vars(args))
+            a.steps, a.autotune = 20, False
+            r = run_resim(a)
+            line["batched"] = {k: r[k] for k in ("metric", "value", "ms_per_step", "speedup_vs_loop",
+                                                 "bitwise_equal_to_loop", "max_div")} | {"loop_ms_per_step": r["loop"]["ms_per_step"]}
+        except Exception as e:  # an extra never blocks the headline line
+            line["batched"] = {"error": str(e)}
+        try:
+            a = argparse.Namespace(**vars(args))
+            a.adj_dirs = 8
+            r = run_adjoint(a)
+            line["adjoint"] = {k: r[k] for k in ("metric", "value", "forward_ms_per_step", "backward_ms_per_step",
+                                                 "adjoint_cost_vs_forward", "gradient_run_cost_vs_forward",
+                                                 "fd_check")}
+        except Exception as e:
+            line["adjoint"] = {"error": str(e)}
+        torch.cuda.set_stream(torch.cuda.default_stream())
     if args.cpu_baseline:
         try:
             cn = min(n, args.cpu_n)
@@ -721,12 +761,15 @@ def main():
     ap.add_argument("--adj-ckpt", type=int, default=10)
     ap.add_argument("--adj-dirs", type=int, default=32)
     ap.add_argument("--adj-eps", type=float, default=1e-5)
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the batched and adjoint summaries of the default line")
     ap.add_argument("--autotune", action="store_true", help="resim: autotune the batched stage kernels first")
     args = ap.parse_args()
-    if args.workload == "resim" and args.impl != "reference":
-        return run_resim(args)
-    if args.workload == "adjoint" and args.impl != "reference":
-        return run_adjoint(args)
+    if args.workload in ("resim", "adjoint") and args.impl != "reference":
+        line = run_resim(args) if args.workload == "resim" else run_adjoint(args)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
