@@ -172,6 +172,27 @@ module ns_gpu
       real(c_double), intent(out) :: max_div
     end function
 
+    ! --- re-simulation error metrics and err_file writer (:813-834, :913-931) ----
+    integer(c_int) function ns_error_metrics(h, u_sub, v_sub, w_sub, p_sub, out) bind(C, name="ns_error_metrics")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: u_sub(*), v_sub(*), w_sub(*), p_sub(*)
+      real(c_double), intent(out) :: out(12)     ! rms_vel(1:4), err_vel(1:8)
+    end function
+
+    integer(c_int) function ns_batch_error_metrics(b, parent, out) bind(C, name="ns_batch_error_metrics")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b, parent
+      real(c_double), intent(out) :: out(*)      ! 12 per subdomain
+    end function
+
+    integer(c_int) function ns_write_err_csv(path, kind, nrows, rows) bind(C, name="ns_write_err_csv")
+      import :: c_int, c_char, c_double
+      character(kind=c_char), intent(in) :: path(*)   ! NUL-terminated
+      integer(c_int), value :: kind, nrows            ! kind 0: err_vel (8 columns), 1: rms_vel (4)
+      real(c_double), intent(in) :: rows(*)           ! row-major: rows(col + ncol*j)
+    end function
+
     ! --- discrete adjoint (no counterpart in the reference) -----------------------
     integer(c_int) function ns_adj_forward(h, nsteps, ckpt_every) bind(C, name="ns_adj_forward")
       import :: c_int, c_ptr

@@ -281,6 +281,36 @@ int ns_batch_get_config(const ns_batch* b, ns_batch_config* out);
 int ns_spline_weights(const double* knots, int n_knots, double t, int* first, double* w);
 
 /* ------------------------------------------------------------------------
+ * Re-simulation error metrics and the err_file writer
+ * (re_simulation_sub_tstep_interBC_combine.f90:813-834, :913-931).
+ *
+ * out[0..3]  = rms(u_ref), rms(v_ref), rms(w_ref), rms(p_ref)   (rms_vel(1..4))
+ * out[4..7]  = maxval(|x - x_ref|) / rms(x_ref) for u, v, w, p  (err_vel(1..4))
+ * out[8..10] = mean(|x - x_ref|) / rms(x_ref) for u, v, w       (err_vel(5..7))
+ * out[11]    = maxval(|oz - oz_ref|) / rms(oz_ref),              (err_vel(8))
+ *              oz = diff(v,1,1)/dx - diff(u,1,2)/dy on (nx+1, ny+1, nz+2)
+ * over the full padded arrays, mean = sum/size, rms = sqrt(sum(a*a)/size)
+ * (other_utility.f90:110-129); reduced on the device.
+ * ------------------------------------------------------------------------ */
+
+/* The session's current u, v, w, p against host reference arrays of the
+ * same shapes (the parent's sub-block u_sub, v_sub, w_sub, p_sub at the
+ * same time step).  Uses the step's scratch fields: call between steps. */
+int ns_error_metrics(ns_handle* h, const double* u_ref, const double* v_ref, const double* w_ref, const double* p_ref,
+                     double* out);
+
+/* Every subdomain of a batch against the parent session's current state
+ * over its index maps (u_sub = u(idx_xu, idx_yu, idx_zu),
+ * big_periodic_3D.f90:20-25,665-669): out[12 * i + q]. */
+int ns_batch_error_metrics(ns_batch* b, const ns_handle* parent, double* out);
+
+/* Write err_vel (kind 0: time_step + 8 columns, rows of err_vel(1..8)) or
+ * rms_vel (kind 1: time_step + 4 columns) in the reference's CSV format:
+ * the header line, then "j,<ES12.5E2>,..." for row j = 0 .. nrows-1.
+ * Host-only; needs no GPU. */
+int ns_write_err_csv(const char* path, int kind, int nrows, const double* rows);
+
+/* ------------------------------------------------------------------------
  * Adjoint tier: the discrete adjoint of the periodic step.
  *
  * The reference has no adjoint; this is the transpose of the tangent-linear

@@ -5,7 +5,7 @@ include/ns_gpu.h); this package only loads it and mirrors the reference's
 step interface on the host.
 """
 from .api import (AB2, AB2_CN, EULER, FACE_ORDER, Batch, NSError, Session, make_batch_config,  # noqa: F401
-                  make_config, shapes, spline_weights)
+                  make_config, shapes, spline_weights, write_err_csv)
 
 __all__ = ["Session", "Batch", "make_config", "make_batch_config", "spline_weights", "shapes", "NSError", "EULER",
-           "AB2", "AB2_CN", "FACE_ORDER"]
+           "AB2", "AB2_CN", "FACE_ORDER", "write_err_csv"]

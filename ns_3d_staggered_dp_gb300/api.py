@@ -199,6 +199,15 @@ class Session:
         self._check(self.lib.ns_adi(self.h, _ptr(us), _ptr(vs), _ptr(ws)))
         return us, vs, ws
 
+    def error_metrics(self, u_ref, v_ref, w_ref, p_ref):
+        """rms_vel(1..4) + err_vel(1..8) of the current state against reference
+        arrays (ns_error_metrics, re_simulation_sub_tstep_interBC_combine.f90:813-834)."""
+        sh = self.shapes
+        arrs = [_f(u_ref, sh["u"]), _f(v_ref, sh["v"]), _f(w_ref, sh["w"]), _f(p_ref, sh["p"])]
+        out = np.zeros(12)
+        self._check(self.lib.ns_error_metrics(self.h, *[_ptr(a) for a in arrs], _ptr(out)))
+        return out
+
     # adjoint tier ------------------------------------------------------------
     def adj_forward(self, nsteps, ckpt_every):
         """Run nsteps steps keeping a checkpoint every ckpt_every steps (ns_adj_forward)."""
@@ -358,3 +367,23 @@ class Batch:
 
     def set_stream(self, stream_handle: int):
         self._check(self.lib.ns_batch_set_stream(self.h, C.c_void_p(stream_handle)))
+
+    def error_metrics(self, parent: "Session"):
+        """(n, 12): rms_vel(1..4) + err_vel(1..8) of every subdomain against the
+        parent's current state over its index maps (ns_batch_error_metrics)."""
+        out = np.zeros((len(self.subs), 12))
+        self._check(self.lib.ns_batch_error_metrics(self.h, parent.h, _ptr(out)))
+        return out
+
+
+def write_err_csv(path, kind, rows):
+    """err_vel (kind 0, 8 columns) or rms_vel (kind 1, 4 columns) file in the
+    reference's format (ns_write_err_csv)."""
+    lib = _lib.load()
+    r = np.ascontiguousarray(rows, dtype=np.float64)
+    ncol = 8 if kind == 0 else 4
+    if r.ndim != 2 or r.shape[1] != ncol:
+        raise NSError(6, f"rows must be (n, {ncol})")
+    s = lib.ns_write_err_csv(str(path).encode(), int(kind), r.shape[0], _ptr(r))
+    if s != 0:
+        raise NSError(s, f"cannot write {path}")

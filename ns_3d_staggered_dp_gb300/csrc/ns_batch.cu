@@ -1069,6 +1069,39 @@ int ns_batch_max_div(ns_batch* b, int i, double* out) {
   return NS_OK;
 }
 
+int ns_batch_error_metrics(ns_batch* b, const ns_handle* parent, double* out) {
+  if (!b || !parent || !out) return NS_ERR_ARG;
+  const Layout& Lp = parent->L;
+  std::vector<MetricBox> boxes(b->n);
+  for (int i = 0; i < b->n; ++i) {
+    const ns_subdomain& d = b->desc[i];
+    if (d.x0 + d.nx > Lp.nx + 1 || d.y0 + d.ny > Lp.ny + 1 || d.z0 + d.nz > Lp.nz + 1)
+      return bfail(b, NS_ERR_SHAPE, "subdomain " + std::to_string(i) + " does not fit inside the parent");
+    MetricBox& B = boxes[i];
+    B.La = b->geo[i].L;
+    B.Lb = Lp;
+    for (int f = 0; f < 4; ++f) B.a[f] = b->geo[i].fld[f];
+    B.b[0] = parent->u; B.b[1] = parent->v; B.b[2] = parent->w; B.b[3] = parent->p;
+    B.ox = d.x0 - 1; B.oy = d.y0 - 1; B.oz = d.z0 - 1;
+    B.idx = 1.0 / b->cfg.dx; B.idy = 1.0 / b->cfg.dy;
+  }
+  cudaEvent_t ev;
+  NB_CUDA(b, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaEventRecord(ev, parent->stream);
+  cudaStreamWaitEvent(b->stream, ev, 0);
+  MetricBox* dbox = nullptr;
+  cudaError_t e = cudaMallocAsync(&dbox, sizeof(MetricBox) * b->n, b->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dbox, boxes.data(), sizeof(MetricBox) * b->n, cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = launch_metrics(dbox, boxes, out, b->stream);
+  if (dbox) cudaFreeAsync(dbox, b->stream);
+  cudaEventRecord(ev, b->stream);
+  cudaStreamWaitEvent(parent->stream, ev, 0);
+  cudaEventDestroy(ev);
+  b->launches += 1;
+  if (e != cudaSuccess) return bfail(b, NS_ERR_CUDA, std::string("metrics: ") + cudaGetErrorString(e));
+  return NS_OK;
+}
+
 int ns_batch_autotune(ns_batch* b, int reps) {
   if (!b) return NS_ERR_ARG;
   if (reps < 1) reps = 3;

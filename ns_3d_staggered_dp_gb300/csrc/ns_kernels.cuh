@@ -1,5 +1,7 @@
 // Kernel argument blocks and launchers of the FP64 staggered step.
 #pragma once
+#include <vector>
+
 #include "ns_internal.cuh"
 
 namespace ns {
@@ -261,6 +263,21 @@ cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st);
 // Batched correction over the items (sub, 256-element chunk bx of the box).
 cudaError_t launch_correct_batch(const CorrectArgs* tab, const BatchItem* items, int n_items, int grid,
                                  cudaStream_t st);
+
+// Re-simulation error metrics (ns_metrics.cu): one box compares fields a
+// (layout La) with reference fields b (layout Lb) at slot offset (ox, oy, oz).
+struct MetricBox {
+  Layout La;
+  Layout Lb;
+  const double* a[4];  // u, v, w, p
+  const double* b[4];
+  int ox, oy, oz;
+  double idx, idy;     // 1/dx, 1/dy (vorticity)
+};
+// Reduce the boxes (dev_boxes: device copy of host_boxes) and fill out[12 * box + q]:
+// rms of the reference u, v, w, p, then err_vel(1..8).  Synchronises st.
+cudaError_t launch_metrics(const MetricBox* dev_boxes, const std::vector<MetricBox>& host_boxes, double* out,
+                           cudaStream_t st);
 
 // max|div u| over the interior and probe value (diagnostic).
 cudaError_t launch_diag(const Layout& L, const double* u, const double* v, const double* w, double idx, double idy,

@@ -854,6 +854,36 @@ def extract_sub(field, which, maps):
     return field[np.ix_(ix, iy, iz)].copy()
 
 
+def error_metrics(u, v, w, p, u_sub, v_sub, w_sub, p_sub, dx, dy):
+    """Post-processing of a re-simulated step against the parent's sub-block.
+    re_simulation_sub_tstep_interBC_combine.f90:826-833 with mean/rms of
+    other_utility.f90:110-129.  Returns rms_vel(1..4) + err_vel(1..8)."""
+    oz = diff(v, 1, 1) / dx - diff(u, 1, 2) / dy
+    oz_sub = diff(v_sub, 1, 1) / dx - diff(u_sub, 1, 2) / dy
+    r = [rms(a) for a in (u_sub, v_sub, w_sub, p_sub)]
+    e = [np.max(np.abs(a - b)) / rr for a, b, rr in zip((u, v, w, p), (u_sub, v_sub, w_sub, p_sub), r)]
+    e += [mean(np.abs(a - b)) / rr for a, b, rr in zip((u, v, w), (u_sub, v_sub, w_sub), r[:3])]
+    e.append(np.max(np.abs(oz - oz_sub)) / rms(oz_sub))
+    return np.array(r + e)
+
+
+def write_err_csv(path, kind, rows):
+    """err_vel (kind 0) / rms_vel (kind 1) text files.  re_simulation_sub_tstep_interBC_combine.f90:913-931:
+    a header, then 'j,' and ES12.5E2 fields per row."""
+    head = ("time_step, rel_err_u, rel_err_v, rel_err_w, rel_err_p, rel_err_u_m, rel_err_v_m, rel_err_w_m, rel_err_p_m"
+            if kind == 0 else "time_step, rms_u, rms_v, rms_w, rms_p")
+    with open(path, "w") as f:
+        f.write(head + "\n")
+        for j, row in enumerate(rows):
+            f.write(str(j) + "".join("," + es12_5e2(x) for x in row) + "\n")
+
+
+def es12_5e2(x):
+    """Fortran ES12.5E2: d.ddddd mantissa, two-digit exponent, right-justified in 12 columns."""
+    m, e = f"{float(x):.5E}".split("E")
+    return f"{m}E{int(e):+03d}".rjust(12)
+
+
 # ---------------------------------------------------------------------------
 # The step
 # ---------------------------------------------------------------------------

@@ -70,3 +70,25 @@ def test_create_rejects_bad_configs_before_touching_the_gpu(lib):
     L.ns_config_default(ctypes.byref(c), 30, 32, 32)   # not a supported FFT size
     assert L.ns_create(ctypes.byref(c), ctypes.byref(h)) == 1
     assert L.ns_create(None, ctypes.byref(h)) == 6
+
+
+def test_err_csv_writer_matches_the_reference_format(tmp_path):
+    """ns_write_err_csv is host code: the err_vel / rms_vel files of
+    re_simulation_sub_tstep_interBC_combine.f90:913-931, byte for byte as the
+    oracle's restatement writes them."""
+    import numpy as np
+
+    from ns_3d_staggered_dp_gb300 import write_err_csv
+    from oracle import ns_oracle as O
+    rng = np.random.default_rng(3)
+    for kind, ncol in ((0, 8), (1, 4)):
+        rows = np.abs(rng.standard_normal((6, ncol))) * 10.0 ** rng.integers(-14, 3, (6, ncol))
+        rows[0, 0] = 0.0
+        rows[1, 1] = -2.5e-7
+        a, b = tmp_path / f"lib_{kind}.txt", tmp_path / f"oracle_{kind}.txt"
+        write_err_csv(a, kind, rows)
+        O.write_err_csv(b, kind, rows)
+        assert a.read_bytes() == b.read_bytes()
+    first = (tmp_path / "lib_0.txt").read_text().splitlines()
+    assert first[0].startswith("time_step, rel_err_u,")
+    assert first[1].startswith("0, 0.00000E+00,")

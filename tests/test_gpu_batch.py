@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 from oracle import ns_oracle as O
-from tests.helpers import rel_l2
+from tests.helpers import random_state, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -163,6 +163,10 @@ def test_batch_p1_replay_of_the_parent(pbc):
                 ref = O.extract_sub(ps[k], k, maps)
                 err = rel_l2(got[k], ref)
                 assert err < P1_TOL, (i, k, err)
+        # the err_vel columns the reference logs for this replay (max and mean
+        # relative errors, vorticity error) stay at rounding level
+        m = b.error_metrics(parent)
+        assert np.all(m[:, 4:] < 1e-9), m[:, 4:]
     parent.close()
 
 
@@ -185,3 +189,34 @@ def test_batch_rejects_bad_input():
     with make_batch([(1, 1, 1, 16, 16, 16, 1)], 4) as b:
         with pytest.raises(NSError):
             b.advance(0.0)  # no snapshot yet
+
+
+def test_error_metrics_session_and_batch_match_the_oracle():
+    """rms_vel / err_vel of re_simulation_sub_tstep_interBC_combine.f90:813-834
+    reduced on the device: a session against perturbed host arrays, and every
+    subdomain of a batch against the parent over its index maps."""
+    from ns_3d_staggered_dp_gb300 import Batch, Session, make_config
+    n = 32
+    h = 2 * np.pi / n
+    cfg = O.Config(n, n, n, nu=0.01, dt=0.01, scheme=O.AB2)
+    st = random_state(cfg, 71)
+    rng = np.random.default_rng(72)
+    pert = [a + 1e-3 * rng.standard_normal(a.shape) for a in (st.u, st.v, st.w, st.p)]
+    with Session(make_config(n, n, n, nu=0.01, dt=0.01, scheme=1, dp_flag=1)) as par:
+        par.set_state(st.u, st.v, st.w, st.p)
+        got = par.error_metrics(*pert)
+        ref = O.error_metrics(st.u, st.v, st.w, st.p, *pert, h, h)
+        assert np.allclose(got, ref, rtol=1e-12, atol=0)
+        par.step(2)
+        subs = [(3, 5, 2, 16, 8, 24, 1), (10, 1, 9, 8, 16, 16, 2)]
+        with Batch(subs, scheme=1, bc=2, pbc=3, nu=0.01, dt0=0.01, dx=h, dy=h, dz=h, n_slots=4) as b:
+            b.init_from_parent(par)
+            par.step(1)  # the parent moves on: the subdomains now differ from it
+            got = b.error_metrics(par)
+            full = par.get_state(history=False)
+            for i, (x0, y0, z0, nx, ny, nz, _) in enumerate(subs):
+                sd = b.get_state(i, history=False)
+                maps = O.subdomain_index_maps(x0, y0, z0, nx, ny, nz)
+                parent_sub = [O.extract_sub(full[k], k, maps) for k in ("u", "v", "w", "p")]
+                ref = O.error_metrics(sd["u"], sd["v"], sd["w"], sd["p"], *parent_sub, h, h)
+                assert np.allclose(got[i], ref, rtol=1e-12, atol=0), (i, got[i], ref)
