@@ -193,6 +193,14 @@ module ns_gpu
       real(c_double), intent(in) :: rows(*)           ! row-major: rows(col + ncol*j)
     end function
 
+    integer(c_int) function ns_spectrum(h, k, E, count, props) bind(C, name="ns_spectrum")
+      import :: c_int, c_ptr, c_double, c_long_long
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: k(*), E(*)         ! nx/2 shells (PowerSpec.m)
+      integer(c_long_long), intent(out) :: count(*)
+      real(c_double), intent(out) :: props(10)          ! SpecProp.m, KolmoScale.m, lambda, Re_lambda
+    end function
+
     ! --- discrete adjoint (no counterpart in the reference) -----------------------
     integer(c_int) function ns_adj_forward(h, nsteps, ckpt_every) bind(C, name="ns_adj_forward")
       import :: c_int, c_ptr

@@ -310,6 +310,19 @@ int ns_batch_error_metrics(ns_batch* b, const ns_handle* parent, double* out);
  * Host-only; needs no GPU. */
 int ns_write_err_csv(const char* path, int kind, int nrows, const double* rows);
 
+/* Energy spectrum and turbulence statistics of the session's current
+ * velocity (MATLAB_post_processing/PowerSpec.m, SpecProp.m, KolmoScale.m as
+ * Post_processing_main.m:29-41 chains them), computed on the device from
+ * the cell-centred velocity with the Poisson solve's FFT passes.  Cubic,
+ * triply periodic boxes only (NS_ERR_SHAPE / NS_ERR_UNSUPPORTED_BC).
+ *   k[N-1], E[N-1], count[N-1]: shell N = 1 .. nx/2 (k = N 2 pi / lx), the
+ *       spectrum of PowerSpec and the number of modes in the shell;
+ *   props[0..9]: dissipation, kin_Sp, kin_Ph, kin_E, up (SpecProp), eta,
+ *       u_eta, tau (KolmoScale), lambda = sqrt(15 nu up^2 / eps),
+ *       Re_lambda = up lambda / nu.
+ * Uses the step's scratch fields: call between steps. */
+int ns_spectrum(ns_handle* h, double* k, double* E, long long* count, double* props);
+
 /* ------------------------------------------------------------------------
  * Adjoint tier: the discrete adjoint of the periodic step.
  *

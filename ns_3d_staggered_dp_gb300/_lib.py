@@ -99,6 +99,7 @@ SIGNATURES = {
     "ns_error_metrics": (C.c_int, [C.c_void_p] + [_DP] * 5),
     "ns_batch_error_metrics": (C.c_int, [C.c_void_p, C.c_void_p, _DP]),
     "ns_write_err_csv": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _DP]),
+    "ns_spectrum": (C.c_int, [C.c_void_p, _DP, _DP, C.POINTER(C.c_longlong), _DP]),
     "ns_adj_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ns_adj_backward": (C.c_int, [C.c_void_p] + [_DP] * 9),
 }

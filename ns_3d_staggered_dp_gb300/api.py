@@ -208,6 +208,19 @@ class Session:
         self._check(self.lib.ns_error_metrics(self.h, *[_ptr(a) for a in arrs], _ptr(out)))
         return out
 
+    SPECTRUM_PROPS = ("dissipation", "kin_Sp", "kin_Ph", "kin_E", "up", "eta", "u_eta", "tau", "lambda",
+                      "Re_lambda")
+
+    def spectrum(self):
+        """(k, E, count, props) of the current velocity (ns_spectrum): the shell
+        spectrum of PowerSpec.m and the statistics of SpecProp.m / KolmoScale.m."""
+        n = self.cfg.nx // 2
+        k, E, props = np.zeros(n), np.zeros(n), np.zeros(10)
+        cnt = np.zeros(n, dtype=np.int64)
+        self._check(self.lib.ns_spectrum(self.h, _ptr(k), _ptr(E), cnt.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                         _ptr(props)))
+        return k, E, cnt, dict(zip(self.SPECTRUM_PROPS, props))
+
     # adjoint tier ------------------------------------------------------------
     def adj_forward(self, nsteps, ckpt_every):
         """Run nsteps steps keeping a checkpoint every ckpt_every steps (ns_adj_forward)."""

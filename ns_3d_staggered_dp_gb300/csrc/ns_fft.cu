@@ -574,6 +574,32 @@ bool fft_size_supported(int nx, int ny, int nz) {
   return ok(nx) && ok(ny) && ok(nz);
 }
 
+// Forward 3D transform of a cell field (d.rhs, cell slots) of an all-periodic
+// plan into spec: r2c along x (the split leaves every bin times 2), then
+// complex FFTs along y and z.
+cudaError_t launch_fft_forward3(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st,
+                                const Marker& mk) {
+  if (P.kind[0] != 0 || P.kind[1] != 0 || P.kind[2] != 0 || !d.rhs) return cudaErrorInvalidValue;
+  const FOne c{d.one, d.mzero};
+  cudaError_t e = cudaSuccess;
+#define X_FWD(n) e = launch_x_fwd<(n) / 2>(P, d, spec, st)
+  NS_SIZE_SWITCH(P.nx, X_FWD)
+#undef X_FWD
+  if (e != cudaSuccess) return e;
+  mk("fft_x_fwd");
+#define Y_FWD(n) e = launch_yz<1, (n), -1>(P, spec, c, st)
+  NS_SIZE_SWITCH(P.ny, Y_FWD)
+#undef Y_FWD
+  if (e != cudaSuccess) return e;
+  mk("fft_y_fwd");
+#define Z_FWD(n) e = launch_yz<2, (n), -1>(P, spec, c, st)
+  NS_SIZE_SWITCH(P.nz, Z_FWD)
+#undef Z_FWD
+  if (e != cudaSuccess) return e;
+  mk("fft_z_fwd");
+  return e;
+}
+
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk) {
   const FOne c{d.one, d.mzero};

@@ -217,6 +217,9 @@ struct DivArgs {
   double one, mzero;
   const double* rhs;     // non-null: transform this right-hand side (cell slots) instead of div(u*)/dt
 };
+// Forward 3D FFT of the cell field d.rhs (all-periodic plan): spec = 2 x DFT.
+cudaError_t launch_fft_forward3(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st,
+                                const Marker& mk);
 // The spectral solve (FFT and dense axes mixed), divergence to dp interior.
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk);

@@ -884,6 +884,53 @@ def es12_5e2(x):
     return f"{m}E{int(e):+03d}".rjust(12)
 
 
+def cell_centred(u, v, w):
+    """u_p, v_p, w_p: face averages at the interior cells.  Post_processing_main.m:29-31."""
+    return ((u[:-1, 1:-1, 1:-1] + u[1:, 1:-1, 1:-1]) / 2, (v[1:-1, :-1, 1:-1] + v[1:-1, 1:, 1:-1]) / 2,
+            (w[1:-1, 1:-1, :-1] + w[1:-1, 1:-1, 1:]) / 2)
+
+
+def power_spec(u, v, w, L):
+    """Shell-summed energy spectrum of an even-sized cube.  PowerSpec.m (MATLAB_post_processing),
+    with its shell tests evaluated in floating point as the script does."""
+    dim = u.shape[0]
+    m = [(np.abs(np.fft.fftn(a)) / dim ** 3) ** 2 for a in (u, v, w)]
+    rx = np.arange(dim) - dim / 2 + 1
+    R = np.roll(rx, dim // 2 + 1)                       # circshift(rx', dim/2+1)
+    r = np.sqrt(R[:, None, None] ** 2 + R[None, :, None] ** 2 + R[None, None, :] ** 2)
+    dx = 2 * np.pi / L
+    k_end = dim // 2
+    k = np.arange(1, k_end + 1) * dx
+    spectrum = np.zeros(k_end)
+    count = np.zeros(k_end, dtype=np.int64)
+    rd = r * dx
+
+    def put(N, pick):
+        spectrum[N] = sum(float(np.sum(mm[pick])) for mm in m)
+        count[N] = int(np.count_nonzero(pick))
+
+    for N in range(1, k_end - 1):                      # MATLAB N = 2 .. k_end-1
+        put(N, (rd <= (k[N + 1] + k[N]) / 2) & (rd > (k[N] + k[N - 1]) / 2))
+    put(0, rd <= (k[1] + k[0]) / 2)
+    put(k_end - 1, (rd > (k[-1] + k[-2]) / 2) & (rd <= k[-1]))
+    E = spectrum * 2 * np.pi * k ** 2 / (count * dx ** 3)
+    return k, E, count, dx, m
+
+
+def spec_prop(E, k, nu, u, v, w, dim, dx, m):
+    """SpecProp.m, KolmoScale.m and the Taylor-scale lines of Post_processing_main.m:36-40."""
+    kin_sp = float(np.sum(E) * dx)
+    diss = float(np.sum(2 * nu * k ** 2 * E) * dx)
+    s = float(np.sum(u ** 2 + v ** 2 + w ** 2))
+    up = np.sqrt(s / 3 / dim ** 3)
+    kin_ph = 0.5 * s / dim ** 3
+    kin_e = 0.5 * sum(float(np.sum(mm)) for mm in m)
+    eta = (nu ** 3 / diss) ** 0.25
+    lam = np.sqrt(15 * nu * up ** 2 / diss)
+    return {"dissipation": diss, "kin_Sp": kin_sp, "kin_Ph": kin_ph, "kin_E": kin_e, "up": up, "eta": eta,
+            "u_eta": (nu * diss) ** 0.25, "tau": (nu / diss) ** 0.5, "lambda": lam, "Re_lambda": up * lam / nu}
+
+
 # ---------------------------------------------------------------------------
 # The step
 # ---------------------------------------------------------------------------

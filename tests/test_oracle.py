@@ -180,3 +180,17 @@ def test_subdomain_index_maps():
     assert len(m["yu"]) == 34 and m["yu"][-1] == 49
     assert len(m["zw"]) == 33 and len(m["xp"]) == 34
     assert m["xu"].dtype == np.int64
+
+
+def test_power_spec_single_mode_and_parseval():
+    """PowerSpec.m / SpecProp.m restated: a cos(2x) field puts all its energy
+    in shell 2, and kin_E (spectral) equals kin_Ph (physical)."""
+    n = 16
+    x = (np.arange(n) + 0.5) * 2 * np.pi / n
+    u = np.cos(2 * x)[:, None, None] * np.ones((n, n, n))
+    z = np.zeros((n, n, n))
+    k, E, c, dk, m = O.power_spec(u, z, z, 2 * np.pi)
+    others = np.delete(E, 1)
+    assert E[1] > 0 and np.all(np.abs(others) < 1e-25 * E[1])
+    p = O.spec_prop(E, k, 0.01, u, z, z, n, dk, m)
+    assert abs(p["kin_E"] - p["kin_Ph"]) < 1e-14 and abs(p["kin_Ph"] - 0.25) < 1e-14
