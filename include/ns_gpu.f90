@@ -88,6 +88,15 @@ module ns_gpu
       integer(c_int), value :: nsteps
     end function
 
+    integer(c_int) function ns_step_host(h, u, v, w, p, rx, ry, rz, uo, vo, wo, po, rxo, ryo, rzo) &
+        bind(C, name="ns_step_host")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: u(*), v(*), w(*)
+      real(c_double), intent(in), optional :: p(*), rx(*), ry(*), rz(*)
+      real(c_double), intent(out), optional :: uo(*), vo(*), wo(*), po(*), rxo(*), ryo(*), rzo(*)
+    end function
+
     integer(c_int) function ns_get_diag(h, d) bind(C, name="ns_get_diag")
       import :: c_int, c_ptr, ns_diag
       type(c_ptr), value :: h

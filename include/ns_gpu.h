@@ -114,6 +114,19 @@ int ns_set_state(ns_handle* h, const double* u, const double* v, const double* w
 int ns_get_state(ns_handle* h, double* u, double* v, double* w, double* p,
                  double* rhs_x_prev, double* rhs_y_prev, double* rhs_z_prev);
 
+/* One step of a driver that keeps its state on the host: the state in, one
+ * step, the state out, in one call (the loop body of
+ * big_periodic_3D.f90:326-567 with host arrays).  Transfers run on a copy
+ * stream and overlap the step: the AB2 history is copied out while the ADI
+ * sweeps and the Poisson solve run.  u, v, w are required; p is read only
+ * with dp_flag = 1 (with dp_flag = 0 the step overwrites p with dp); NULL
+ * history inputs mean the Euler start.  Any output may be NULL.  The output
+ * arrays may be the input arrays.  Equivalent to ns_set_state + ns_step(h, 1)
+ * + ns_get_state, bit for bit. */
+int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w, const double* p,
+                 const double* rhs_x_prev, const double* rhs_y_prev, const double* rhs_z_prev, double* u_out,
+                 double* v_out, double* w_out, double* p_out, double* rhs_x_out, double* rhs_y_out, double* rhs_z_out);
+
 /* Boundary faces, in the reference shapes and order of get_velpr_bc's
  * outputs (NS_functions.f90:414-420):
  *   bx_u_1, bx_u_nx, by_u_1, by_u_ny, bz_u_1, bz_u_nz,

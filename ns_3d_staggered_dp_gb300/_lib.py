@@ -70,6 +70,7 @@ SIGNATURES = {
     "ns_get_state": (C.c_int, [C.c_void_p] + [_DP] * 7),
     "ns_set_faces": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_DP)]),
     "ns_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ns_step_host": (C.c_int, [C.c_void_p] + [_DP] * 14),
     "ns_get_diag": (C.c_int, [C.c_void_p, C.POINTER(NSDiag)]),
     "ns_cal_conv": (C.c_int, [C.c_void_p] + [_DP] * 6),
     "ns_cal_diff": (C.c_int, [C.c_void_p] + [_DP] * 6),

@@ -135,6 +135,19 @@ class Session:
     def step(self, n=1):
         self._check(self.lib.ns_step(self.h, n))
 
+    def step_host(self, u, v, w, p, rhs_prev=None, out=None):
+        """One step of host-resident state (ns_step_host): returns the state
+        dict (u, v, w, p, hx, hy, hz); `out` may hold preallocated arrays."""
+        sh = self.shapes
+        ins = [_f(u, sh["u"]), _f(v, sh["v"]), _f(w, sh["w"]), _f(p, sh["p"])]
+        hist = [None] * 3 if rhs_prev is None else [_f(rhs_prev[0], sh["u"]), _f(rhs_prev[1], sh["v"]),
+                                                     _f(rhs_prev[2], sh["w"])]
+        keys = ("u", "v", "w", "p", "hx", "hy", "hz")
+        shp = (sh["u"], sh["v"], sh["w"], sh["p"], sh["u"], sh["v"], sh["w"])
+        res = {k: (out[k] if out is not None and k in out else np.zeros(sp, order="F")) for k, sp in zip(keys, shp)}
+        self._check(self.lib.ns_step_host(self.h, *[_ptr(a) for a in ins + hist], *[_ptr(res[k]) for k in keys]))
+        return res
+
     def synchronize(self):
         self._check(self.lib.ns_synchronize(self.h))
 

@@ -248,12 +248,25 @@ cudaError_t ensure_xfer(ns_handle* h) {
   for (int b = 0; b < 2; ++b) {
     if ((e = cudaEventCreateWithFlags(&h->ev_full[b], cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&h->ev_aux[b], cudaEventDisableTiming)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
+// The history's interior ranges (0-based reference indices) of field f:
+// entries outside them are returned as zero.
+void hist_range(const ns_config& c, int f, int lo[3], int hi[3]) {
+  for (int ax = 0; ax < 3; ++ax) {
+    const int na = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
+    if (ax == f) { lo[ax] = c.bc[ax] == 1 ? 0 : 1; hi[ax] = na - 1; }
+    else { lo[ax] = 1; hi[ax] = na; }
+  }
+}
+
+
+
 cudaError_t pack_launch(ns_handle* h, double* field, double* stage, int f, bool to_field, const int* lo = nullptr,
-                        const int* hi = nullptr) {
+                        const int* hi = nullptr, cudaStream_t stream = nullptr) {
   const ns_config& c = h->cfg;
   PackArgs a{};
   a.L = h->L;
@@ -269,12 +282,34 @@ cudaError_t pack_launch(ns_handle* h, double* field, double* stage, int f, bool 
   }
   const long long n = (long long)a.ex * a.ey * a.ez;
   const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  field_pack_kernel<<<grid, 256, 0, h->stream>>>(a);
+  field_pack_kernel<<<grid, 256, 0, stream ? stream : h->stream>>>(a);
   return cudaGetLastError();
 }
 
 inline size_t field_bytes(const ns_config& c, int f) {
   return sizeof(double) * ext_of(c, f, 0) * ext_of(c, f, 1) * ext_of(c, f, 2);
+}
+
+// On the copy stream: gather each field into a staging buffer and copy it
+// out, the two buffers in turn (ordered by the stream itself).
+cudaError_t d2h_on_xfer(ns_handle* h, int n, double* const* dst, const double* const* src, const int* fid,
+                        const bool* zero_hist, int& next_buf) {
+  double* buf[2] = {h->stage, h->stage2};
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < n; ++q) {
+    double* b = buf[next_buf];
+    next_buf ^= 1;
+    int lo[3], hi[3];
+    hist_range(h->cfg, fid[q], lo, hi);
+    const bool z = zero_hist && zero_hist[q];
+    if ((e = pack_launch(h, const_cast<double*>(src[q]), b, fid[q], false, z ? lo : nullptr, z ? hi : nullptr,
+                         h->xfer)) != cudaSuccess)
+      return e;
+    if ((e = cudaMemcpyAsync(dst[q], b, field_bytes(h->cfg, fid[q]), cudaMemcpyDeviceToHost, h->xfer)) !=
+        cudaSuccess)
+      return e;
+  }
+  return e;
 }
 
 // n fields in: copies on the copy stream, scatters on the handle's stream,
@@ -315,11 +350,7 @@ cudaError_t d2h_fields(ns_handle* h, int n, double* const* dst, const double* co
     const int b = q & 1, f = fid[q];
     if ((e = cudaStreamWaitEvent(h->stream, h->ev_free[b], 0)) != cudaSuccess) return e;
     int lo[3], hi[3];
-    for (int ax = 0; ax < 3; ++ax) {  // the history's interior ranges (0-based reference indices)
-      const int na = ax == 0 ? c.nx : (ax == 1 ? c.ny : c.nz);
-      if (ax == f) { lo[ax] = c.bc[ax] == 1 ? 0 : 1; hi[ax] = na - 1; }
-      else { lo[ax] = 1; hi[ax] = na; }
-    }
+    hist_range(c, f, lo, hi);
     const bool z = zero_hist && zero_hist[q];
     if ((e = pack_launch(h, const_cast<double*>(src[q]), buf[b], f, false, z ? lo : nullptr, z ? hi : nullptr)) !=
         cudaSuccess)
@@ -527,11 +558,12 @@ int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
   return NS_OK;
 }
 
-int enqueue_step(ns_handle* h, bool first) {
+int enqueue_step(ns_handle* h, bool first, cudaEvent_t after_predict = nullptr) {
   const ns_config& c = h->cfg;
   PredictArgs a = predict_args(h);
   NS_CUDA(h, launch_predict(a, c.scheme, first, c.dp_flag != 0, 0, h->stream));
   mark(h, "predict");
+  if (after_predict) NS_CUDA(h, cudaEventRecord(after_predict, h->stream));
   if (c.scheme == NS_AB2_CN) {
     int s = enqueue_adi(h);
     if (s) return s;
@@ -751,6 +783,7 @@ void free_all(ns_handle* h) {
   for (int b = 0; b < 2; ++b) {
     if (h->ev_full[b]) cudaEventDestroy(h->ev_full[b]);
     if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
+    if (h->ev_aux[b]) cudaEventDestroy(h->ev_aux[b]);
   }
   if (h->tw) cudaFree(h->tw);
   if (h->diag_bits) cudaFree(h->diag_bits);
@@ -912,6 +945,69 @@ int ns_get_state(ns_handle* h, double* u, double* v, double* w, double* p, doubl
     ++n;
   }
   NS_CUDA(h, d2h_fields(h, n, dst, src, fid, zero));
+  return NS_OK;
+}
+
+int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w, const double* p, const double* hx,
+                 const double* hy, const double* hz, double* uo, double* vo, double* wo, double* po, double* hxo,
+                 double* hyo, double* hzo) {
+  if (!h || !u || !v || !w) return fail(h, NS_ERR_ARG, "u, v, w are required");
+  const ns_config& c = h->cfg;
+  if (c.dp_flag && !p) return fail(h, NS_ERR_ARG, "p is required with dp_flag = 1");
+  NS_CUDA(h, ensure_xfer(h));
+  const bool hist = hx && hy && hz;
+  // state in: the fields the step reads (p only with dp_flag = 1)
+  double* dst[7];
+  const double* src[7];
+  int fid[7];
+  int n = 0;
+  auto add = [&](double* d, const double* s_, int f) { dst[n] = d; src[n] = s_; fid[n] = f; ++n; };
+  add(h->u, u, 0); add(h->v, v, 1); add(h->w, w, 2);
+  if (hist) { add(h->hx, hx, 0); add(h->hy, hy, 1); add(h->hz, hz, 2); }
+  if (c.dp_flag) add(h->p, p, 3);
+  NS_CUDA(h, h2d_fields(h, n, dst, src, fid));
+  NS_CUDA(h, launch_extra_slots(h->L, h->u, h->v, h->w, c.bc, h->stream));
+  if (!hist) {
+    NS_CUDA(h, cudaMemsetAsync(h->hx, 0, h->L.fsize * sizeof(double), h->stream));
+    NS_CUDA(h, cudaMemsetAsync(h->hy, 0, h->L.fsize * sizeof(double), h->stream));
+    NS_CUDA(h, cudaMemsetAsync(h->hz, 0, h->L.fsize * sizeof(double), h->stream));
+  }
+  // the step, eagerly, with an event once the history is final
+  const bool first = !hist && c.scheme != NS_EULER;
+  int s = enqueue_step(h, first, h->ev_aux[0]);
+  if (s) return s;
+  NS_CUDA(h, cudaEventRecord(h->ev_aux[1], h->stream));
+  // state out on the copy stream: the history while the rest of the step runs
+  int nb = 0;
+  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_aux[0], 0));
+  {
+    double* od[3];
+    const double* os[3];
+    int of[3];
+    bool oz[3];
+    int m = 0;
+    double* want[3] = {hxo, hyo, hzo};
+    const double* have[3] = {h->hx, h->hy, h->hz};
+    for (int q = 0; q < 3; ++q)
+      if (want[q]) { od[m] = want[q]; os[m] = have[q]; of[m] = q; oz[m] = true; ++m; }
+    NS_CUDA(h, d2h_on_xfer(h, m, od, os, of, oz, nb));
+  }
+  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_aux[1], 0));
+  {
+    double* od[4];
+    const double* os[4];
+    int of[4];
+    int m = 0;
+    double* want[4] = {uo, vo, wo, po};
+    const double* have[4] = {h->u, h->v, h->w, h->p};
+    for (int q = 0; q < 4; ++q)
+      if (want[q]) { od[m] = want[q]; os[m] = have[q]; of[m] = q; ++m; }
+    NS_CUDA(h, d2h_on_xfer(h, m, od, os, of, nullptr, nb));
+  }
+  NS_CUDA(h, cudaStreamSynchronize(h->xfer));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->first_pending = false;
+  h->steps = 1;
   return NS_OK;
 }
 

@@ -30,6 +30,7 @@ struct ns_handle {
   double* stage2 = nullptr;  // second staging buffer (multi-field transfers)
   cudaStream_t xfer = nullptr;  // copy stream of the multi-field transfers
   cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  cudaEvent_t ev_aux[2] = {nullptr, nullptr};  // ns_step_host: history final, step done
   double* inv_lam = nullptr;
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
   ns::FftPlan plan{};

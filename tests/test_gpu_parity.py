@@ -155,3 +155,19 @@ def test_determinism():
             s.step(4)
             outs.append(s.get_state())
     assert all(np.array_equal(outs[0][k], outs[1][k]) for k in ("u", "v", "w", "p"))
+
+
+@pytest.mark.parametrize("scheme,dpf", [(O.AB2_CN, 0), (O.AB2, 1)])
+def test_step_host_equals_set_step_get(scheme, dpf):
+    """ns_step_host (transfers overlapped with the step) gives the bits of
+    ns_set_state + ns_step + ns_get_state, from an Euler start and with history."""
+    cfg = O.Config(32, 16, 32, nu=0.02, dt=0.01, scheme=scheme, dp_flag=dpf)
+    st = random_state(cfg, 91, history=True)
+    with session(cfg) as s:
+        for hist in (None, (st.px, st.py, st.pz)):
+            s.set_state(st.u, st.v, st.w, st.p, hist)
+            s.step(1)
+            ref = s.get_state()
+            got = s.step_host(st.u, st.v, st.w, st.p, hist)
+            for k in ref:
+                assert np.array_equal(got[k], ref[k]), k
