@@ -59,6 +59,16 @@ __device__ __forceinline__ double fadd(const FOne& c, double a, double b) { retu
 __device__ __forceinline__ double fsub(const FOne& c, double a, double b) { return fma(b, -c.one, a); }
 __device__ __forceinline__ double fmul(const FOne& c, double a, double b) { return fma(a, b, c.mzero); }
 
+// Asynchronous 8-byte global -> shared copies (cp.async, L1-allocating) and
+// their commit groups.
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Error word on the device (bit flags).
 enum : unsigned { ERRW_NONFINITE = 1u, ERRW_BOUNDS = 2u, ERRW_TIMEOUT = 4u };
 

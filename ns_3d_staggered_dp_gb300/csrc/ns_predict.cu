@@ -37,11 +37,12 @@ constexpr int SYH = TY + 2;  // smem rows: y in [j0-1, j0+TY]
 constexpr int PXW = TX + 1;  // product row width: x in [i0-1, i0+31]
 constexpr int PYH = TY + 1;  // product rows: y in [j0-1, j0+TY-1]
 
+constexpr int RING = 4;       // planes k-1, k, k+1 in use, k+2 in flight
+
 struct PredSmem {
-  double u[3][SYH][SXW];
-  double v[3][SYH][SXW];
-  double w[3][SYH][SXW];
-  double p[3][SYH][SXW];
+  double u[RING][SYH][SXW];
+  double v[RING][SYH][SXW];
+  double w[RING][SYH][SXW];
   double sx2[PYH][PXW];
   double sy2[PYH][PXW];
   double sz2[2][PYH][PXW];
@@ -52,11 +53,11 @@ struct PredSmem {
 
 __device__ __forceinline__ int clampi(int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); }
 
-// Load plane k (clamped into the box) of u, v, w (and p) into ring slot s.
-template <bool DPF>
-__device__ __forceinline__ void load_plane(PredSmem& S, const Layout& L, const double* __restrict__ u,
-                                           const double* __restrict__ v, const double* __restrict__ w,
-                                           const double* __restrict__ p, int i0, int j0, int k, int s, int ps) {
+// Start copying plane k (clamped into the box) of u, v, w into ring slot s
+// (cp.async; the caller commits the group).
+__device__ __forceinline__ void issue_plane(PredSmem& S, const Layout& L, const double* __restrict__ u,
+                                            const double* __restrict__ v, const double* __restrict__ w, int i0,
+                                            int j0, int k, int s) {
   const int kk = clampi(k, 0, L.nz + 1);
   const int nthr = blockDim.x * blockDim.y;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
@@ -65,10 +66,9 @@ __device__ __forceinline__ void load_plane(PredSmem& S, const Layout& L, const d
     const int gi = clampi(i0 - 1 + xx, 0, L.nx + 1);
     const int gj = clampi(j0 - 1 + yy, 0, L.ny + 1);
     const long long g = L.at(gi, gj, kk);
-    S.u[s][yy][xx] = __ldg(u + g);
-    S.v[s][yy][xx] = __ldg(v + g);
-    S.w[s][yy][xx] = __ldg(w + g);
-    if (DPF) S.p[ps][yy][xx] = __ldg(p + g);
+    cp_async8(&S.u[s][yy][xx], u + g);
+    cp_async8(&S.v[s][yy][xx], v + g);
+    cp_async8(&S.w[s][yy][xx], w + g);
   }
 }
 
@@ -130,14 +130,19 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
   const int xa = lane + 1;
   const int yb = wy;
 
-  // Warm-up: planes k0-1 and k0 in ring slots, products at z-face k0.
-  load_plane<DPF>(S, L, a.u, a.v, a.w, a.p, i0, j0, k0 - 1, (k0 - 1) % 3, (k0 - 1) % 3);
-  load_plane<DPF>(S, L, a.u, a.v, a.w, a.p, i0, j0, k0, k0 % 3, k0 % 3);
+  // Warm-up: planes k0-1 and k0 (one copy group) and k0+1 (a second one);
+  // products at z-face k0 once the first group has landed.
+  issue_plane(S, L, a.u, a.v, a.w, i0, j0, k0 - 1, (k0 - 1) & 3);
+  issue_plane(S, L, a.u, a.v, a.w, i0, j0, k0, k0 & 3);
+  cp_async_commit();
+  issue_plane(S, L, a.u, a.v, a.w, i0, j0, k0 + 1, (k0 + 1) & 3);
+  cp_async_commit();
+  cp_async_wait<1>();
   __syncthreads();
   if (MODE != 2) {
-    products_zface(S, c, xa, yb, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
+    products_zface(S, c, xa, yb, (k0 - 1) & 3, k0 & 3, (k0 - 1) & 1);
     // low x-halo position of every row, by warp 0 (one partially active pass)
-    if (wy == 0 && lane <= TY) products_zface(S, c, 0, lane, (k0 - 1) % 3, k0 % 3, (k0 - 1) & 1);
+    if (wy == 0 && lane <= TY) products_zface(S, c, 0, lane, (k0 - 1) & 3, k0 & 3, (k0 - 1) & 1);
   }
 
   const int i = i0 + lane;
@@ -148,10 +153,14 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
   const bool act_v = in_xy && (j >= a.vlo);
 
   for (int k = k0; k < k1; ++k) {
-    const int s0 = k % 3, s1 = (k + 1) % 3, sm = (k + 2) % 3;  // planes k, k+1, k-1
+    const int s0 = k & 3, s1 = (k + 1) & 3, sm = (k + 3) & 3;  // planes k, k+1, k-1
     const int pb = k & 1, pbm = (k - 1) & 1;
-    load_plane<DPF>(S, L, a.u, a.v, a.w, a.p, i0, j0, k + 1, s1, s1);
+    // plane k+1 has landed and every thread is done with plane k-2, whose
+    // slot receives plane k+2 while this plane is computed
+    cp_async_wait<0>();
     __syncthreads();
+    issue_plane(S, L, a.u, a.v, a.w, i0, j0, k + 2, (k + 2) & 3);
+    cp_async_commit();
     if (MODE != 2) {
       products(S, c, xa, yb, s0, s1, pb);
       if (wy == 0 && lane <= TY) products(S, c, 0, lane, s0, s1, pb);
@@ -182,7 +191,7 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
           out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, uc))));
         } else {
           out = predictor_combine<SCHEME, FIRST>(a, c, uc, sWE, sSN, sBT, C, a.hx, g);
-          if (DPF) out = fma(a.gpx, fsub(c, S.p[s0][yb][xa], S.p[s0][yb][xa - 1]), out);
+          if (DPF) out = fma(a.gpx, fsub(c, __ldg(a.p + g), __ldg(a.p + g - 1)), out);
         }
         a.us[g] = out;
       }
@@ -208,7 +217,7 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
           out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, vc))));
         } else {
           out = predictor_combine<SCHEME, FIRST>(a, c, vc, sWE, sSN, sBT, C, a.hy, g);
-          if (DPF) out = fma(a.gpy, fsub(c, S.p[s0][yb][xa], S.p[s0][yb - 1][xa]), out);
+          if (DPF) out = fma(a.gpy, fsub(c, __ldg(a.p + g), __ldg(a.p + g - L.sy)), out);
         }
         a.vs[g] = out;
       }
@@ -234,13 +243,13 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
           out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, wc))));
         } else {
           out = predictor_combine<SCHEME, FIRST>(a, c, wc, sWE, sSN, sBT, C, a.hz, g);
-          if (DPF) out = fma(a.gpz, fsub(c, S.p[s0][yb][xa], S.p[sm][yb][xa]), out);
+          if (DPF) out = fma(a.gpz, fsub(c, __ldg(a.p + g), __ldg(a.p + g - L.sz)), out);
         }
         a.ws[g] = out;
       }
     }
-    __syncthreads();
   }
+  cp_async_wait<0>();  // nothing left in flight when the tile is done
 }
 
 template <int SCHEME, bool FIRST, bool DPF, int MODE>
