@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(32 * XW) adi_x_kernel(AdiArgs a) {
   const int n1 = L.ny + 2, n2 = L.nz + 2;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int j0 = (blockIdx.x * XW + warp) * 32;
-  const int k = blockIdx.y;
+  const int k = blockIdx.y + a.z0;
   if (j0 >= n1) return;
   const int nl = min(32, n1 - j0);
   double* sb = sh[warp];
@@ -164,7 +164,9 @@ template <int AXIS, int PD>
 __global__ void __launch_bounds__(128) adi_line_kernel(AdiArgs a) {
   const Layout L = a.L;
   const int n1 = (AXIS == 0) ? L.ny + 2 : L.nx + 2;
-  const int n2 = (AXIS == 2) ? L.ny + 2 : L.nz + 2;
+  // the y sweep may be limited to the lines of z slots [z0, z1)
+  const int zlo = (AXIS == 1 && a.z1 > 0) ? a.z0 : 0;
+  const int n2 = (AXIS == 2) ? L.ny + 2 : ((AXIS == 1 && a.z1 > 0) ? a.z1 - a.z0 : L.nz + 2);
   const int per_field = n1 * n2;
   const int total = 3 * per_field;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(128) adi_line_kernel(AdiArgs a) {
     const int tl = t - fld * per_field;
     const LineSys& S = a.sys[fld];
     long long base, st;
-    line_of<AXIS>(L, tl % n1, tl / n1, base, st);
+    line_of<AXIS>(L, tl % n1, zlo + tl / n1, base, st);
     const double* __restrict__ src = a.src[fld] + base;
     double* __restrict__ dst = a.dst[fld] + base;
     const double* lf = S.l + S.pad;
@@ -185,8 +187,9 @@ __global__ void __launch_bounds__(128) adi_line_kernel(AdiArgs a) {
     if (S.periodic) {
       r_lo = 0.0; r_hi = 0.0;
     } else {
-      r_lo = a.face_lo[fld] ? __ldg(a.face_lo[fld] + tl) : 0.0;
-      r_hi = a.face_hi[fld] ? __ldg(a.face_hi[fld] + tl) : 0.0;
+      const int pl = tl + zlo * n1;  // index in the full face plane
+      r_lo = a.face_lo[fld] ? __ldg(a.face_lo[fld] + pl) : 0.0;
+      r_hi = a.face_hi[fld] ? __ldg(a.face_hi[fld] + pl) : 0.0;
     }
     const bool per = S.periodic != 0;
     auto rhs = [&](int e) -> double {
@@ -251,14 +254,16 @@ cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     const int n1 = a.L.nx + 2;
-    const int n2 = (axis == 2) ? a.L.ny + 2 : a.L.nz + 2;
+    const int n2 = (axis == 2) ? a.L.ny + 2 : (a.z1 > 0 ? a.z1 - a.z0 : a.L.nz + 2);
+    if (n2 <= 0) return cudaSuccess;
     const int need = (3 * n1 * n2 + 127) / 128;
     const int grid = std::min(need, 8 * std::max(1, nsm));
     if (axis == 1) adi_line_kernel<1, 8><<<grid, 128, 0, st>>>(a);
     else adi_line_kernel<2, 8><<<grid, 128, 0, st>>>(a);
     return cudaGetLastError();
   }
-  const int n1 = a.L.ny + 2, n2 = a.L.nz + 2;
+  const int n1 = a.L.ny + 2, n2 = a.z1 > 0 ? a.z1 - a.z0 : a.L.nz + 2;
+  if (n2 <= 0) return cudaSuccess;
   dim3 grid((n1 + 32 * XW - 1) / (32 * XW), n2, 3);
   adi_x_kernel<<<grid, 32 * XW, 0, st>>>(a);
   return cudaGetLastError();

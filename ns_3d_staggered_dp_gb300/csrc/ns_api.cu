@@ -212,12 +212,15 @@ struct PackArgs {
   int ox, oy, oz;   // slot of reference index 0 per axis
   int to_field;     // 1: stage -> field, 0: field -> stage
   int lo[3], hi[3]; // kept range on the way out (others zero)
+  int z_lo, z_hi;   // reference planes [z_lo, z_hi) moved
 };
 
 __global__ void __launch_bounds__(256) field_pack_kernel(PackArgs a) {
-  const long long n = (long long)a.ex * a.ey * a.ez;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
+  const long long plane = (long long)a.ex * a.ey;
+  const long long n = plane * (a.z_hi - a.z_lo);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long t = q + plane * a.z_lo;
     const int i = (int)(t % a.ex);
     const long long r = t / a.ex;
     const int j = (int)(r % a.ey);
@@ -228,6 +231,24 @@ __global__ void __launch_bounds__(256) field_pack_kernel(PackArgs a) {
     } else {
       const bool keep = i >= a.lo[0] && i <= a.hi[0] && j >= a.lo[1] && j <= a.hi[1] && k >= a.lo[2] && k <= a.hi[2];
       a.stage[t] = keep ? a.field[g] : 0.0;
+    }
+  }
+}
+
+// The extra face slot 0 of u along x and of v along y (periodic axes) on
+// z slots [z0, z1): the slab-wise part of launch_extra_slots.
+__global__ void __launch_bounds__(256) extra_xy_kernel(Layout L, double* u, double* v, int perx, int pery, int z0,
+                                                       int z1) {
+  const int nyp = L.ny + 2, nxp = L.nx + 2, per = nyp + nxp;
+  const long long n = (long long)(z1 - z0) * per;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int k = z0 + (int)(t / per);
+    const int r = (int)(t % per);
+    if (r < nyp) {
+      if (perx) u[L.at(0, r, k)] = u[L.at(L.nx, r, k)];
+    } else if (pery) {
+      const int i = r - nyp;
+      v[L.at(i, 0, k)] = v[L.at(i, L.ny, k)];
     }
   }
 }
@@ -266,7 +287,7 @@ void hist_range(const ns_config& c, int f, int lo[3], int hi[3]) {
 
 
 cudaError_t pack_launch(ns_handle* h, double* field, double* stage, int f, bool to_field, const int* lo = nullptr,
-                        const int* hi = nullptr, cudaStream_t stream = nullptr) {
+                        const int* hi = nullptr, cudaStream_t stream = nullptr, int z_lo = 0, int z_hi = -1) {
   const ns_config& c = h->cfg;
   PackArgs a{};
   a.L = h->L;
@@ -280,7 +301,10 @@ cudaError_t pack_launch(ns_handle* h, double* field, double* stage, int f, bool 
     a.lo[q] = lo ? lo[q] : 0;
     a.hi[q] = hi ? hi[q] : ext[q] - 1;
   }
-  const long long n = (long long)a.ex * a.ey * a.ez;
+  a.z_lo = z_lo;
+  a.z_hi = z_hi < 0 ? a.ez : z_hi;
+  if (a.z_hi <= a.z_lo) return cudaSuccess;
+  const long long n = (long long)a.ex * a.ey * (a.z_hi - a.z_lo);
   const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
   field_pack_kernel<<<grid, 256, 0, stream ? stream : h->stream>>>(a);
   return cudaGetLastError();
@@ -515,20 +539,24 @@ namespace {
 // The three sweeps with fixed buffer roles: x reads A (the predictor's
 // output) and writes B, y reads B and writes A, z reads A and writes B, so
 // the final u*, v*, w* are in B on every step (and in every captured graph).
-int enqueue_adi(ns_handle* h) {
+AdiArgs adi_args(ns_handle* h, int ax) {
   double* A[3] = {h->us, h->vs, h->ws};
   double* B[3] = {h->us2, h->vs2, h->ws2};
+  AdiArgs a{};
+  a.L = h->L;
+  for (int f = 0; f < 3; ++f) {
+    a.src[f] = (ax == 1) ? B[f] : A[f];
+    a.dst[f] = (ax == 1) ? A[f] : B[f];
+    a.sys[f] = h->sys[ax][f];
+    a.face_lo[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][0] : nullptr;
+    a.face_hi[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][1] : nullptr;
+  }
+  return a;
+}
+
+int enqueue_adi(ns_handle* h) {
   for (int ax = 0; ax < 3; ++ax) {
-    AdiArgs a{};
-    a.L = h->L;
-    for (int f = 0; f < 3; ++f) {
-      a.src[f] = (ax == 1) ? B[f] : A[f];
-      a.dst[f] = (ax == 1) ? A[f] : B[f];
-      a.sys[f] = h->sys[ax][f];
-      a.face_lo[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][0] : nullptr;
-      a.face_hi[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][1] : nullptr;
-    }
-    NS_CUDA(h, launch_adi(ax, a, h->stream));
+    NS_CUDA(h, launch_adi(ax, adi_args(h, ax), h->stream));
     mark(h, ax == 0 ? "adi_x" : (ax == 1 ? "adi_y" : "adi_z"));
   }
   return NS_OK;
@@ -558,15 +586,26 @@ int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
   return NS_OK;
 }
 
+// Everything after the predictor: the ADI sweeps (x and y unless already
+// done plane by plane) or the BC fill, the Poisson solve, the correction.
+int enqueue_tail(ns_handle* h, bool adi_xy_done);
+
 int enqueue_step(ns_handle* h, bool first, cudaEvent_t after_predict = nullptr) {
   const ns_config& c = h->cfg;
   PredictArgs a = predict_args(h);
   NS_CUDA(h, launch_predict(a, c.scheme, first, c.dp_flag != 0, 0, h->stream));
   mark(h, "predict");
   if (after_predict) NS_CUDA(h, cudaEventRecord(after_predict, h->stream));
+  return enqueue_tail(h, false);
+}
+
+int enqueue_tail(ns_handle* h, bool adi_xy_done) {
+  const ns_config& c = h->cfg;
   if (c.scheme == NS_AB2_CN) {
-    int s = enqueue_adi(h);
-    if (s) return s;
+    for (int ax = adi_xy_done ? 2 : 0; ax < 3; ++ax) {
+      NS_CUDA(h, launch_adi(ax, adi_args(h, ax), h->stream));
+      mark(h, ax == 0 ? "adi_x" : (ax == 1 ? "adi_y" : "adi_z"));
+    }
   } else {
     NS_CUDA(h, launch_vel_bc(h->L, h->us, h->vs, h->ws, h->faces[0], c.bc, h->stream));
     mark(h, "vel_bc", 3);
@@ -785,6 +824,9 @@ void free_all(ns_handle* h) {
     if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
     if (h->ev_aux[b]) cudaEventDestroy(h->ev_aux[b]);
   }
+  for (double* b : h->stage_f)
+    if (b) cudaFree(b);
+  for (cudaEvent_t e : h->ev_slab) cudaEventDestroy(e);
   if (h->tw) cudaFree(h->tw);
   if (h->diag_bits) cudaFree(h->diag_bits);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -955,27 +997,117 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   const ns_config& c = h->cfg;
   if (c.dp_flag && !p) return fail(h, NS_ERR_ARG, "p is required with dp_flag = 1");
   NS_CUDA(h, ensure_xfer(h));
+  const Layout& L = h->L;
+  const int nz = c.nz;
   const bool hist = hx && hy && hz;
-  // state in: the fields the step reads (p only with dp_flag = 1)
-  double* dst[7];
-  const double* src[7];
-  int fid[7];
-  int n = 0;
-  auto add = [&](double* d, const double* s_, int f) { dst[n] = d; src[n] = s_; fid[n] = f; ++n; };
-  add(h->u, u, 0); add(h->v, v, 1); add(h->w, w, 2);
-  if (hist) { add(h->hx, hx, 0); add(h->hy, hy, 1); add(h->hz, hz, 2); }
-  if (c.dp_flag) add(h->p, p, 3);
-  NS_CUDA(h, h2d_fields(h, n, dst, src, fid));
-  NS_CUDA(h, launch_extra_slots(h->L, h->u, h->v, h->w, c.bc, h->stream));
-  if (!hist) {
-    NS_CUDA(h, cudaMemsetAsync(h->hx, 0, h->L.fsize * sizeof(double), h->stream));
-    NS_CUDA(h, cudaMemsetAsync(h->hy, 0, h->L.fsize * sizeof(double), h->stream));
-    NS_CUDA(h, cudaMemsetAsync(h->hz, 0, h->L.fsize * sizeof(double), h->stream));
+  // state in: the fields the step reads (p only with dp_flag = 1), one staging buffer each
+  struct In { double* dev; const double* host; int fid; int q; };
+  std::vector<In> in = {{h->u, u, 0, 0}, {h->v, v, 1, 1}, {h->w, w, 2, 2}};
+  if (hist) { in.push_back({h->hx, hx, 0, 4}); in.push_back({h->hy, hy, 1, 5}); in.push_back({h->hz, hz, 2, 6}); }
+  if (c.dp_flag) in.push_back({h->p, p, 3, 3});
+  for (const In& f : in)
+    if (!h->stage_f[f.q]) NS_CUDA(h, cudaMalloc(&h->stage_f[f.q], field_bytes(c, f.fid)));
+  // z-slabs of 4 predictor chunks: copy, scatter, predict, x and y sweeps of
+  // slab s run while slab s+1 is being copied.  (Slabs of 2 chunks left each
+  // predictor launch under one wave of CTAs, and the compute of a slab
+  // outlasted its copy.)
+  const int KC = predict_chunk_planes();
+  const int S = 4 * KC, nslab = (nz + 2 + S - 1) / S;
+  while ((int)h->ev_slab.size() < nslab + 1) {
+    cudaEvent_t e;
+    NS_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->ev_slab.push_back(e);
   }
-  // the step, eagerly, with an event once the history is final
+  if (!hist) {
+    NS_CUDA(h, cudaMemsetAsync(h->hx, 0, L.fsize * sizeof(double), h->stream));
+    NS_CUDA(h, cudaMemsetAsync(h->hy, 0, L.fsize * sizeof(double), h->stream));
+    NS_CUDA(h, cudaMemsetAsync(h->hz, 0, L.fsize * sizeof(double), h->stream));
+  }
+  NS_CUDA(h, cudaEventRecord(h->ev_slab[nslab], h->stream));
+  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[nslab], 0));
+  auto plane_bytes = [&](int fid) {
+    return sizeof(double) * (size_t)ext_of(c, fid, 0) * ext_of(c, fid, 1);
+  };
+  // reference planes [r0, r1) of field f that hold z slots [lo, hi)
+  auto ref_range = [&](const In& f, int lo, int hi, int& r0, int& r1) {
+    const int off = (f.fid == 2) ? 1 : 0;  // w-type fields: slot k is reference plane k - 1
+    const int ez = ext_of(c, f.fid, 2);
+    r0 = std::max(lo - off, 0);
+    r1 = std::min(hi - off, ez);
+  };
+  auto copy_in = [&](const In& f, int r0, int r1) -> cudaError_t {
+    if (r1 <= r0) return cudaSuccess;
+    const size_t pb = plane_bytes(f.fid), pd = pb / sizeof(double);
+    return cudaMemcpyAsync(h->stage_f[f.q] + pd * r0, f.host + pd * r0, pb * (r1 - r0), cudaMemcpyHostToDevice,
+                           h->xfer);
+  };
+  // The periodic image w(slot 0) = w(slot nz) is read by the first chunk:
+  // bring the w plane of slot nz in ahead of the slabs.
+  const bool zper = c.bc[2] == 1;
+  if (zper) {
+    NS_CUDA(h, copy_in(in[2], nz - 1, nz));
+    NS_CUDA(h, cudaEventRecord(h->ev_full[0], h->xfer));
+    NS_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_full[0], 0));
+    NS_CUDA(h, pack_launch(h, h->w, h->stage_f[2], 2, true, nullptr, nullptr, nullptr, nz - 1, nz));
+    const int zonly[3] = {0, 0, 1};
+    NS_CUDA(h, launch_extra_slots(L, h->u, h->v, h->w, zonly, h->stream));
+  }
+  for (int s = 0; s < nslab; ++s) {
+    const int lo = s * S, hi = std::min(nz + 2, (s + 1) * S);
+    for (const In& f : in) {
+      int r0, r1;
+      ref_range(f, lo, hi, r0, r1);
+      NS_CUDA(h, copy_in(f, r0, r1));
+    }
+    NS_CUDA(h, cudaEventRecord(h->ev_slab[s], h->xfer));
+  }
+  const bool cn = c.scheme == NS_AB2_CN;
   const bool first = !hist && c.scheme != NS_EULER;
-  int s = enqueue_step(h, first, h->ev_aux[0]);
-  if (s) return s;
+  const int nch = (nz + KC - 1) / KC;
+  int c_next = 0, xy_done = 0;
+  PredictArgs pa = predict_args(h);
+  for (int s = 0; s < nslab; ++s) {
+    const int lo = s * S, hi = std::min(nz + 2, (s + 1) * S);
+    NS_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_slab[s], 0));
+    for (const In& f : in) {
+      int r0, r1;
+      ref_range(f, lo, hi, r0, r1);
+      NS_CUDA(h, pack_launch(h, f.dev, h->stage_f[f.q], f.fid, true, nullptr, nullptr, nullptr, r0, r1));
+    }
+    {
+      const long long n = (long long)(hi - lo) * (L.nx + L.ny + 4);
+      extra_xy_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 1024), 256, 0, h->stream>>>(
+          L, h->u, h->v, c.bc[0] == 1, c.bc[1] == 1, lo, hi);
+      NS_CUDA(h, cudaGetLastError());
+    }
+    // chunks whose planes (and the two planes above, read by the prefetch) have arrived
+    int c_ready = c_next;
+    while (c_ready < nch) {
+      const int k1 = std::min(1 + KC * (c_ready + 1), nz + 1);
+      if (std::min(k1 + 2, nz + 2) > hi) break;
+      ++c_ready;
+    }
+    if (c_ready > c_next) {
+      NS_CUDA(h, launch_predict_range(pa, c.scheme, first, c.dp_flag != 0, c_next, c_ready, h->stream));
+      mark(h, "predict");
+      c_next = c_ready;
+      if (cn) {  // x and y sweeps of the planes the predictor has finished
+        const int zhi = c_ready == nch ? nz + 2 : 1 + KC * c_ready;
+        for (int ax = 0; ax < 2; ++ax) {
+          AdiArgs a = adi_args(h, ax);
+          a.z0 = xy_done;
+          a.z1 = zhi;
+          NS_CUDA(h, launch_adi(ax, a, h->stream));
+          mark(h, ax == 0 ? "adi_x" : "adi_y");
+        }
+        xy_done = zhi;
+      }
+    }
+  }
+  if (c_next != nch) return fail(h, NS_ERR_ARG, "internal: predictor chunks left after the last slab");
+  NS_CUDA(h, cudaEventRecord(h->ev_aux[0], h->stream));  // the history is final
+  int st = enqueue_tail(h, cn);
+  if (st) return st;
   NS_CUDA(h, cudaEventRecord(h->ev_aux[1], h->stream));
   // state out on the copy stream: the history while the rest of the step runs
   int nb = 0;

@@ -48,6 +48,7 @@ struct PredictArgs {
   double dt, e1, e2;  // AB2: u* = u + e1*rhs + e2*prev
   double gpx, gpy, gpz;  // -dt/dx etc. (dp_flag)
   double ix2, iy2, iz2, lap0;  // diffusion-only mode
+  int bz0;                     // first z-chunk of the launch (chunk ranges of the pipelined host step)
 };
 
 // Combine the stencil pieces into u* and rewrite the AB2 history at g.
@@ -83,6 +84,9 @@ __device__ __forceinline__ double predictor_combine(const PredictArgs& a, const 
 
 size_t predict_smem_bytes();
 cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st);
+// The predictor on z-chunks [c0, c1) only (chunks of predict_chunk_planes() planes from slot 1).
+cudaError_t launch_predict_range(PredictArgs a, int scheme, bool first, bool dpf, int c0, int c1, cudaStream_t st);
+int predict_chunk_planes();
 // Predictor tiles of one box (work items of the batched launch).
 void predict_tiles(const Layout& L, int& gx, int& gy, int& gz);
 // Batched predictor over the items (grid <= 0: one wave of resident CTAs).
@@ -151,6 +155,7 @@ struct AdiArgs {
   LineSys sys[3];        // per field (normal or tangential system)
   const double* face_lo[3];  // BC row values per field (internal-slot planes), NULL -> 0
   const double* face_hi[3];
+  int z0, z1;                // x and y sweeps: only the lines of z slots [z0, z1) (z1 = 0: all)
 };
 cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st);
 

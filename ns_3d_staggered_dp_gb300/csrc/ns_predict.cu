@@ -255,7 +255,8 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
 template <int SCHEME, bool FIRST, bool DPF, int MODE>
 __global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  predict_body<SCHEME, FIRST, DPF, MODE>(a, *reinterpret_cast<PredSmem*>(smem_raw), blockIdx.x, blockIdx.y, blockIdx.z);
+  predict_body<SCHEME, FIRST, DPF, MODE>(a, *reinterpret_cast<PredSmem*>(smem_raw), blockIdx.x, blockIdx.y,
+                                         blockIdx.z + a.bz0);
 }
 
 // Batched: persistent CTAs walk the work items (subdomain, tile) of a batch.
@@ -276,15 +277,32 @@ __global__ void __launch_bounds__(TX*(TY + 1)) predict_batch_kernel(const Predic
 size_t predict_smem_bytes() { return sizeof(PredSmem); }
 
 template <int SCHEME, bool FIRST, bool DPF, int MODE>
-static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st) {
+static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st, int c0 = 0, int c1 = -1) {
   auto kern = predict_kernel<SCHEME, FIRST, DPF, MODE>;
   const size_t sm = sizeof(PredSmem);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  dim3 grid((a.L.nx + TX - 1) / TX, (a.L.ny + TY - 1) / TY, (a.L.nz + KC - 1) / KC);
+  const int nch = (a.L.nz + KC - 1) / KC;
+  if (c1 < 0) c1 = nch;
+  if (c0 < 0 || c1 > nch || c0 >= c1) return c0 == c1 ? cudaSuccess : cudaErrorInvalidValue;
+  PredictArgs b = a;
+  b.bz0 = c0;
+  dim3 grid((a.L.nx + TX - 1) / TX, (a.L.ny + TY - 1) / TY, c1 - c0);
   dim3 block(TX, TY + 1);
-  kern<<<grid, block, sm, st>>>(a);
+  kern<<<grid, block, sm, st>>>(b);
   return cudaGetLastError();
+}
+
+int predict_chunk_planes() { return KC; }
+
+cudaError_t launch_predict_range(PredictArgs a, int scheme, bool first, bool dpf, int c0, int c1, cudaStream_t st) {
+#define NS_PRED_RCASE(S, F, D) \
+  if (scheme == S && first == F && dpf == D) return launch_t<S, F, D, 0>(a, st, c0, c1);
+  NS_PRED_RCASE(0, false, false) NS_PRED_RCASE(0, false, true) NS_PRED_RCASE(0, true, false) NS_PRED_RCASE(0, true, true)
+  NS_PRED_RCASE(1, false, false) NS_PRED_RCASE(1, false, true) NS_PRED_RCASE(1, true, false) NS_PRED_RCASE(1, true, true)
+  NS_PRED_RCASE(2, false, false) NS_PRED_RCASE(2, false, true) NS_PRED_RCASE(2, true, false) NS_PRED_RCASE(2, true, true)
+#undef NS_PRED_RCASE
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st) {

@@ -31,6 +31,8 @@ struct ns_handle {
   cudaStream_t xfer = nullptr;  // copy stream of the multi-field transfers
   cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   cudaEvent_t ev_aux[2] = {nullptr, nullptr};  // ns_step_host: history final, step done
+  double* stage_f[7] = {};                     // ns_step_host: one staging buffer per state field
+  std::vector<cudaEvent_t> ev_slab;            // ns_step_host: one event per z-slab
   double* inv_lam = nullptr;
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
   ns::FftPlan plan{};

@@ -157,11 +157,15 @@ def test_determinism():
     assert all(np.array_equal(outs[0][k], outs[1][k]) for k in ("u", "v", "w", "p"))
 
 
-@pytest.mark.parametrize("scheme,dpf", [(O.AB2_CN, 0), (O.AB2, 1)])
-def test_step_host_equals_set_step_get(scheme, dpf):
-    """ns_step_host (transfers overlapped with the step) gives the bits of
-    ns_set_state + ns_step + ns_get_state, from an Euler start and with history."""
-    cfg = O.Config(32, 16, 32, nu=0.02, dt=0.01, scheme=scheme, dp_flag=dpf)
+@pytest.mark.parametrize("scheme,dpf,walls,n", [(O.AB2_CN, 0, False, (32, 16, 32)), (O.AB2, 1, False, (32, 16, 32)),
+                                                (O.AB2_CN, 0, False, (16, 32, 128)), (O.AB2_CN, 1, True, (32, 16, 64)),
+                                                (O.EULER, 0, False, (16, 16, 64))])
+def test_step_host_equals_set_step_get(scheme, dpf, walls, n):
+    """ns_step_host (z-slabs copied, scattered, predicted and swept in x and y
+    while the next slab is in flight) gives the bits of ns_set_state +
+    ns_step + ns_get_state, from an Euler start and with history."""
+    kw = dict(bc=(1, 2, 1), pbc=(1, 3, 1)) if walls else {}
+    cfg = O.Config(*n, nu=0.02, dt=0.01, scheme=scheme, dp_flag=dpf, **kw)
     st = random_state(cfg, 91, history=True)
     with session(cfg) as s:
         for hist in (None, (st.px, st.py, st.pz)):
