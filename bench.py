@@ -390,6 +390,7 @@ def run_resim(args):
         for b in batches.values():
             b.set_stream(stream.cuda_stream)
         tuned = batches[0].autotune(reps=3) if args.autotune else None
+        stage_ms = None
         t_job0 = time.perf_counter()
         for k in range(1, T + n0 + 7):
             par.step(1)
@@ -416,6 +417,7 @@ def run_resim(args):
             out[m] = {"ms": ms, "value": steady / (ms / 1e3), "launches": b.launch_count() - l0,
                       "clocks": clk.summary()}
         job_sec = time.perf_counter() - t_job0
+        stage_ms = batches[0].profile(reps=3)
         st = [batches[m].get_state(0, history=False) for m in (0, 1)]
         same = all(np.array_equal(st[0][k], st[1][k]) for k in ("u", "v", "w", "p"))
         divs = [batches[0].max_div(i) for i in range(len(subs))]
@@ -438,6 +440,7 @@ def run_resim(args):
         "bitwise_equal_to_loop": same,
         "max_div": max(divs),
         "autotuned_grid": tuned,
+        "stage_ms": stage_ms,
         "clocks": out[0]["clocks"],
         "e2e": {"value": work / job_sec, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                 "path": "whole job: parent steps + snapshot captures + both batches (mode 0 and 1)"},

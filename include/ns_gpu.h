@@ -285,6 +285,11 @@ int ns_batch_launch_count(const ns_batch* b, long long* launches);
 /* Time every stage kernel over a few persistent grid sizes and keep the
  * fastest in the batch's configuration (runs steps: call on a scratch state). */
 int ns_batch_autotune(ns_batch* b, int reps);
+/* Device time of every stage kernel of one regular step (mean over reps
+ * launches, on a copy of the state), in the stage order interp, predict,
+ * vel_bc x/y/z, x forward, y forward, z solve, y inverse, x inverse,
+ * pr_bc x/y/z, correct, hist: ms_per_stage[16] (the last two unused). */
+int ns_batch_profile(ns_batch* b, int reps, double* ms_per_stage);
 int ns_batch_get_config(const ns_batch* b, ns_batch_config* out);
 
 /* Weights of MATLAB interp1(knots, y, t, 'spline') (the not-a-knot cubic

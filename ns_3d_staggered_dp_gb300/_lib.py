@@ -96,6 +96,7 @@ SIGNATURES = {
     "ns_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "ns_batch_autotune": (C.c_int, [C.c_void_p, C.c_int]),
     "ns_batch_get_config": (C.c_int, [C.c_void_p, C.POINTER(NSBatchConfig)]),
+    "ns_batch_profile": (C.c_int, [C.c_void_p, C.c_int, _DP]),
     "ns_spline_weights": (C.c_int, [_DP, C.c_int, C.c_double, C.POINTER(C.c_int), _DP]),
     "ns_error_metrics": (C.c_int, [C.c_void_p] + [_DP] * 5),
     "ns_batch_error_metrics": (C.c_int, [C.c_void_p, C.c_void_p, _DP]),

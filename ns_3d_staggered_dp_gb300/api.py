@@ -394,6 +394,15 @@ class Batch:
     def set_stream(self, stream_handle: int):
         self._check(self.lib.ns_batch_set_stream(self.h, C.c_void_p(stream_handle)))
 
+    STAGES = ("interp", "predict", "vel_bc_x", "vel_bc_y", "vel_bc_z", "x_fwd", "y_fwd", "z_solve", "y_inv",
+              "x_inv", "pr_bc_x", "pr_bc_y", "pr_bc_z", "correct")
+
+    def profile(self, reps=3):
+        """{stage: ms} of one regular step's stage kernels (ns_batch_profile)."""
+        out = np.zeros(16)
+        self._check(self.lib.ns_batch_profile(self.h, int(reps), _ptr(out)))
+        return dict(zip(self.STAGES, out[:len(self.STAGES)]))
+
     def error_metrics(self, parent: "Session"):
         """(n, 12): rms_vel(1..4) + err_vel(1..8) of every subdomain against the
         parent's current state over its index maps (ns_batch_error_metrics)."""

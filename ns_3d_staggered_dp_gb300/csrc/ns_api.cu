@@ -694,6 +694,7 @@ int build_plans(ns_handle* h) {
     std::vector<double> F, G;
     dense_pair(n3[a], c.pbc[a], F, G);
     const int n = n3[a];
+    P.sym[a] = dense_symmetry(n, F, G);
     if (a == 0) {
       std::vector<double> Ft((size_t)n * n), Gt((size_t)n * n);
       for (int r = 0; r < n; ++r)

@@ -658,11 +658,13 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   // ---- size-class tables: dense x (transposed) and y pairs, x and y eigenvalues ----
   std::vector<double> tab;
   std::map<int, size_t> xF, xG, yF, yG, ex, ey;
+  std::map<int, int> ysym, xsym;  // symmetry bits of the y and x pairs per size
   for (int i = 0; i < n; ++i) {
     const int nx = subs[i].nx, ny = subs[i].ny;
     if (!xF.count(nx)) {
       std::vector<double> F, G;
       dense_pair(nx, c.pbc, F, G);
+      xsym[nx] = dense_symmetry(nx, F, G);
       std::vector<double> Ft((size_t)nx * nx), Gt((size_t)nx * nx);
       for (int r = 0; r < nx; ++r)
         for (int q = 0; q < nx; ++q) { Ft[(size_t)q * nx + r] = F[(size_t)r * nx + q]; Gt[(size_t)q * nx + r] = G[(size_t)r * nx + q]; }
@@ -675,6 +677,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     if (!yF.count(ny)) {
       std::vector<double> F, G;
       dense_pair(ny, c.pbc, F, G);
+      ysym[ny] = dense_symmetry(ny, F, G);
       yF[ny] = tab.size(); tab.insert(tab.end(), F.begin(), F.end()); tab.resize(align32(tab.size()));
       yG[ny] = tab.size(); tab.insert(tab.end(), G.begin(), G.end()); tab.resize(align32(tab.size()));
       ey[ny] = tab.size();
@@ -720,6 +723,8 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     S.kind[0] = 1; S.kind[1] = 1; S.kind[2] = 2;
     S.fwd[0] = b->tables + xF[d.nx]; S.inv[0] = b->tables + xG[d.nx];
     S.fwd[1] = b->tables + yF[d.ny]; S.inv[1] = b->tables + yG[d.ny];
+    S.sym[1] = ysym[d.ny];
+    S.sym[0] = xsym[d.nx];
     S.eig_x = b->tables + ex[d.nx];
     S.eig_o = b->tables + ey[d.ny];
     S.tri_h2 = c.dz * c.dz;
@@ -1099,6 +1104,38 @@ int ns_batch_error_metrics(ns_batch* b, const ns_handle* parent, double* out) {
   cudaEventDestroy(ev);
   b->launches += 1;
   if (e != cudaSuccess) return bfail(b, NS_ERR_CUDA, std::string("metrics: ") + cudaGetErrorString(e));
+  return NS_OK;
+}
+
+int ns_batch_profile(ns_batch* b, int reps, double* ms_per_stage) {
+  if (!b || !ms_per_stage) return NS_ERR_ARG;
+  if (reps < 1) reps = 3;
+  // On a copy of the state, as the autotuner: the timed launches rewrite it.
+  double* save = nullptr;
+  NB_CUDA(b, cudaMalloc(&save, b->arena_n * sizeof(double)));
+  NB_CUDA(b, cudaMemcpyAsync(save, b->arena, b->arena_n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int status = NS_OK;
+  for (int q = 0; q < ST_COUNT; ++q) ms_per_stage[q] = 0.0;
+  for (int stage : kStageOrder) {
+    if (stage == ST_HIST) continue;
+    if (launch_stage_kernel(b, 0, stage, false, b->stream) != cudaSuccess) { status = NS_ERR_CUDA; break; }
+    cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < reps; ++r) launch_stage_kernel(b, 0, stage, false, b->stream);
+    cudaEventRecord(e1, b->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) { status = NS_ERR_CUDA; break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms_per_stage[stage] = ms / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaMemcpyAsync(b->arena, save, b->arena_n * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
+  cudaStreamSynchronize(b->stream);
+  cudaFree(save);
+  if (status) return bfail(b, status, "profile launch failed");
   return NS_OK;
 }
 

@@ -24,6 +24,9 @@
 // The divergence kernels add the pressure-BC terms of
 // pr_bc_staggered_modify_rhs (NS_functions.f90:1345-1400) on the first and
 // last cells of every non-periodic axis.
+#include <cmath>
+#include <vector>
+
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
 
@@ -63,6 +66,27 @@ __device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArg
   if (!valid) return;
   const double* __restrict__ FT = S.fwd[0];  // F^T: FT[n * N + kk] = F[kk][n]
   double2* out = spec + (long long)S.nxs * ((j - 1) + (long long)ny * (k - 1));
+  if (S.sym[0] & 1) {
+    // F[k][N-1-n] = (-1)^k F[k][n]: fold the line (s[n] = r[n] + r[N-1-n] at n,
+    // d[n] = r[n] - r[N-1-n] at N-1-n); mode 2q sums F s, mode 2q+1 sums F d
+    const int H = nx / 2;
+    for (int n = lane; n < H; n += 32) {
+      const double a0 = r[n], b0 = r[nx - 1 - n];
+      r[n] = a0 + b0;
+      r[nx - 1 - n] = a0 - b0;
+    }
+    __syncwarp();
+    for (int q = lane; q < H; q += 32) {
+      double a = 0.0, b = 0.0;
+      for (int n = 0; n < H; ++n) {
+        const double2 f = *reinterpret_cast<const double2*>(FT + (long long)n * nx + 2 * q);
+        a = fma(f.x, r[n], a);
+        b = fma(f.y, r[nx - 1 - n], b);
+      }
+      out[q] = make_double2(a, b);
+    }
+    return;
+  }
   for (int q = lane; q < nx / 2; q += 32) {
     double a = 0.0, b = 0.0;
     for (int n = 0; n < nx; ++n) {
@@ -94,6 +118,19 @@ __device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double
   if (!valid) return;
   const double* __restrict__ GT = S.inv[0];  // G^T: GT[kk * N + n] = G[n][kk] (x = G X)
   double* o = dp + L.at(1, j, k);
+  if (S.sym[0] & 2) {
+    // G[N-1-n][k] = (-1)^k G[n][k]: out[n] = E + O, out[N-1-n] = E - O
+    for (int n = lane; n < nx / 2; n += 32) {
+      double e = 0.0, od = 0.0;
+      for (int kk = 0; kk + 1 < nx; kk += 2) {
+        e = fma(__ldg(GT + (long long)kk * nx + n), X[kk], e);
+        od = fma(__ldg(GT + (long long)(kk + 1) * nx + n), X[kk + 1], od);
+      }
+      o[n] = e + od;
+      o[nx - 1 - n] = e - od;
+    }
+    return;
+  }
   for (int n = lane; n < nx; n += 32) {
     double a = 0.0;
     for (int kk = 0; kk < nx; ++kk) a = fma(__ldg(GT + (long long)kk * nx + n), X[kk], a);
@@ -118,8 +155,58 @@ __device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __rest
   if (valid)
     for (int n = t; n < N; n += T) line[n * LPC] = g[(long long)n * st];
   __syncthreads();
-  const double* __restrict__ M = FWD ? S.fwd[AXIS] : S.inv[AXIS];
-  // outputs k = t + T*q
+  const double* __restrict__ M = FWD ? S.fwd[AXIS] : S.inv[AXIS];  // row = output index
+  const bool sym = (S.sym[AXIS] >> (FWD ? 0 : 1)) & 1;
+  if (sym && FWD) {
+    // F[k][N-1-n] = (-1)^k F[k][n]: fold the line into s[n] = x[n] + x[N-1-n]
+    // (kept at n) and d[n] = x[n] - x[N-1-n] (kept at N-1-n); an even mode
+    // then sums F[k][n] s[n], an odd one F[k][n] d[n], over n < N/2.
+    const int H = N / 2;
+    if (valid)
+      for (int n = t; n < H; n += T) {
+        const double2 a = line[n * LPC], b = line[(N - 1 - n) * LPC];
+        line[n * LPC] = make_double2(a.x + b.x, a.y + b.y);
+        line[(N - 1 - n) * LPC] = make_double2(a.x - b.x, a.y - b.y);
+      }
+    __syncthreads();
+    if (!valid) return;
+    for (int kk = t; kk < N; kk += T) {  // kk has the parity of t
+      const double2* src = (kk & 1) ? line + (long long)(N - 1) * LPC : line;
+      const int step = (kk & 1) ? -LPC : LPC;
+      const double* __restrict__ row = M + (long long)kk * N;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int n = 0; n < H; ++n) {
+        const double2 v = src[n * step];
+        const double m = __ldg(row + n);
+        acc.x = fma(m, v.x, acc.x);
+        acc.y = fma(m, v.y, acc.y);
+      }
+      g[(long long)kk * st] = acc;
+    }
+    return;
+  }
+  if (sym) {
+    // G[N-1-n][k] = (-1)^k G[n][k]: even and odd partial sums of row n give
+    // out[n] = E + O and out[N-1-n] = E - O
+    if (!valid) return;
+    const int H = N / 2;
+    for (int r = t; r < H; r += T) {
+      const double* __restrict__ row = M + (long long)r * N;
+      double2 e = make_double2(0.0, 0.0), od = make_double2(0.0, 0.0);
+      for (int c = 0; c + 1 < N; c += 2) {
+        const double2 v0 = line[c * LPC], v1 = line[(c + 1) * LPC];
+        const double m0 = __ldg(row + c), m1 = __ldg(row + c + 1);
+        e.x = fma(m0, v0.x, e.x);
+        e.y = fma(m0, v0.y, e.y);
+        od.x = fma(m1, v1.x, od.x);
+        od.y = fma(m1, v1.y, od.y);
+      }
+      g[(long long)r * st] = make_double2(e.x + od.x, e.y + od.y);
+      g[(long long)(N - 1 - r) * st] = make_double2(e.x - od.x, e.y - od.y);
+    }
+    return;
+  }
+  // general N: the full matrix product, outputs k = t + T*q
   double2 acc[16];
   const int nq = (N + T - 1) / T;
 #pragma unroll
@@ -346,6 +433,21 @@ cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double
   if (fwd) dense_x_fwd_kernel<<<(lines + 3) / 4, 128, sm, st>>>(S, d, spec);
   else dense_x_inv_kernel<<<(lines + 3) / 4, 128, sm, st>>>(S, spec, dp, L);
   return cudaGetLastError();
+}
+
+int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double>& G) {
+  if (n < 2 || n % 2) return 0;
+  double fm = 0.0, gm = 0.0;
+  for (double x : F) fm = std::fmax(fm, std::fabs(x));
+  for (double x : G) gm = std::fmax(gm, std::fabs(x));
+  bool fs = true, gs = true;
+  for (int r = 0; r < n && (fs || gs); ++r)
+    for (int q = 0; q < n; ++q) {
+      const double sg_r = (r & 1) ? -1.0 : 1.0, sg_q = (q & 1) ? -1.0 : 1.0;
+      if (std::fabs(F[(size_t)r * n + (n - 1 - q)] - sg_r * F[(size_t)r * n + q]) > 4e-16 * fm) fs = false;
+      if (std::fabs(G[(size_t)(n - 1 - r) * n + q] - sg_q * G[(size_t)r * n + q]) > 4e-16 * gm) gs = false;
+    }
+  return (fs ? 1 : 0) | (gs ? 2 : 0);
 }
 
 cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st) {

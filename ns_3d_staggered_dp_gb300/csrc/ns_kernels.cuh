@@ -176,6 +176,7 @@ struct FftPlan {
   int kind[3];            // 0: FFT axis, 1: dense transform axis, 2: tridiagonal solve axis (a wall)
   const double* fwd[3];   // dense forward matrices (x: F^T [n][k]; y, z: F [k][n])
   const double* inv[3];   // dense inverse matrices (x: G^T [k][n]; y, z: G [n][k])
+  int sym[3];             // bit 0: F[k][N-1-n] = (-1)^k F[k][n]; bit 1: G[N-1-n][k] = (-1)^k G[n][k]
   int has_mean;           // 1: the singular mode is set to mean_val (after the forward passes)
   double mean_val;        // FFT z solve: the singular entry; tridiagonal solve: the singular line's mean
   const double* mean_dev; // non-null: the line mean is mean_val * (*mean_dev) (a mean_dp set on the device)
@@ -228,6 +229,9 @@ cudaError_t launch_fft_forward3(const FftPlan& P, const DivArgs& d, double2* spe
 // The spectral solve (FFT and dense axes mixed), divergence to dp interior.
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk);
+// Symmetry bits of a dense transform pair of even size n (sym in FftPlan),
+// checked entry by entry on the host (ns_dct.cu).
+int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double>& G);
 // Dense passes (ns_dct.cu): x forward/inverse, y/z forward/inverse.
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                            cudaStream_t st);
