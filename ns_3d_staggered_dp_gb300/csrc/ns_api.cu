@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -215,16 +216,21 @@ struct PackArgs {
   int z_lo, z_hi;   // reference planes [z_lo, z_hi) moved
 };
 
+// IDX: the index type of the flat reference index (32-bit divisions where
+// the moved planes hold fewer than 2^32 entries; 64-bit emulated ones cost
+// more than the copy itself).
+template <typename IDX>
 __global__ void __launch_bounds__(256) field_pack_kernel(PackArgs a) {
-  const long long plane = (long long)a.ex * a.ey;
-  const long long n = plane * (a.z_hi - a.z_lo);
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-       q += (long long)gridDim.x * blockDim.x) {
-    const long long t = q + plane * a.z_lo;
-    const int i = (int)(t % a.ex);
-    const long long r = t / a.ex;
-    const int j = (int)(r % a.ey);
-    const int k = (int)(r / a.ey);
+  const IDX ex = (IDX)a.ex, ey = (IDX)a.ey;
+  const IDX n = ex * ey * (IDX)(a.z_hi - a.z_lo);
+  const long long base = (long long)a.ex * a.ey * a.z_lo;  // flat index of the first moved entry
+  for (IDX q = blockIdx.x * (IDX)blockDim.x + threadIdx.x; q < n; q += (IDX)gridDim.x * blockDim.x) {
+    const IDX r = q / ex;
+    const int i = (int)(q - r * ex);
+    const IDX kk = r / ey;
+    const int j = (int)(r - kk * ey);
+    const int k = a.z_lo + (int)kk;
+    const long long t = base + (long long)q;
     const long long g = a.L.at(a.ox + i, a.oy + j, a.oz + k);
     if (a.to_field) {
       a.field[g] = a.stage[t];
@@ -266,6 +272,7 @@ cudaError_t ensure_xfer(ns_handle* h) {
   const size_t n = (size_t)(h->cfg.nx + 2) * (h->cfg.ny + 2) * (h->cfg.nz + 2);
   if ((e = cudaMalloc(&h->stage2, n * sizeof(double))) != cudaSuccess) return e;
   if ((e = cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking)) != cudaSuccess) return e;
   for (int b = 0; b < 2; ++b) {
     if ((e = cudaEventCreateWithFlags(&h->ev_full[b], cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming)) != cudaSuccess) return e;
@@ -306,34 +313,15 @@ cudaError_t pack_launch(ns_handle* h, double* field, double* stage, int f, bool 
   if (a.z_hi <= a.z_lo) return cudaSuccess;
   const long long n = (long long)a.ex * a.ey * (a.z_hi - a.z_lo);
   const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  field_pack_kernel<<<grid, 256, 0, stream ? stream : h->stream>>>(a);
+  if (n + (long long)grid * 256 < (1LL << 32))
+    field_pack_kernel<unsigned><<<grid, 256, 0, stream ? stream : h->stream>>>(a);
+  else
+    field_pack_kernel<unsigned long long><<<grid, 256, 0, stream ? stream : h->stream>>>(a);
   return cudaGetLastError();
 }
 
 inline size_t field_bytes(const ns_config& c, int f) {
   return sizeof(double) * ext_of(c, f, 0) * ext_of(c, f, 1) * ext_of(c, f, 2);
-}
-
-// On the copy stream: gather each field into a staging buffer and copy it
-// out, the two buffers in turn (ordered by the stream itself).
-cudaError_t d2h_on_xfer(ns_handle* h, int n, double* const* dst, const double* const* src, const int* fid,
-                        const bool* zero_hist, int& next_buf) {
-  double* buf[2] = {h->stage, h->stage2};
-  cudaError_t e = cudaSuccess;
-  for (int q = 0; q < n; ++q) {
-    double* b = buf[next_buf];
-    next_buf ^= 1;
-    int lo[3], hi[3];
-    hist_range(h->cfg, fid[q], lo, hi);
-    const bool z = zero_hist && zero_hist[q];
-    if ((e = pack_launch(h, const_cast<double*>(src[q]), b, fid[q], false, z ? lo : nullptr, z ? hi : nullptr,
-                         h->xfer)) != cudaSuccess)
-      return e;
-    if ((e = cudaMemcpyAsync(dst[q], b, field_bytes(h->cfg, fid[q]), cudaMemcpyDeviceToHost, h->xfer)) !=
-        cudaSuccess)
-      return e;
-  }
-  return e;
 }
 
 // n fields in: copies on the copy stream, scatters on the handle's stream,
@@ -492,6 +480,34 @@ void mark(ns_handle* h, const char* name, int nkernels = 1) {
   }
 }
 void mark_cb(void* ctx, const char* name) { mark(static_cast<ns_handle*>(ctx), name); }
+
+// Phase trace of ns_step_host: a timed event on stream st (NS_TRACE only),
+// named name, or "name s [lo,hi)" for a slab.
+void trace_mark(ns_handle* h, cudaStream_t st, const char* name, int s = -1, int lo = 0, int hi = 0) {
+  if (!h->trace) return;
+  char buf[96];
+  if (s >= 0) std::snprintf(buf, sizeof buf, "%s %d [%d,%d)", name, s, lo, hi);
+  else std::snprintf(buf, sizeof buf, "%s", name);
+  const size_t n = h->trace_names.size();
+  if (n == h->trace_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    h->trace_pool.push_back(e);
+  }
+  if (cudaEventRecord(h->trace_pool[n], st) == cudaSuccess) h->trace_names.push_back(buf);
+}
+
+// Print the phases recorded since the first trace_mark, in ms from it, and reset.
+void trace_flush(ns_handle* h) {
+  if (!h->trace || h->trace_names.empty()) return;
+  cudaDeviceSynchronize();
+  for (size_t i = 0; i < h->trace_names.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->trace_pool[0], h->trace_pool[i]);
+    std::fprintf(stderr, "ns_trace %-22s %9.3f ms\n", h->trace_names[i].c_str(), ms);
+  }
+  h->trace_names.clear();
+}
 Marker marker(ns_handle* h) {
   Marker m;
   m.fn = mark_cb;
@@ -570,7 +586,7 @@ inline void final_star(ns_handle* h, const double** fs) {
   fs[2] = cn ? h->ws2 : h->ws;
 }
 
-int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
+DivArgs div_args(ns_handle* h, const double* rhs) {
   const ns_config& c = h->cfg;
   DivArgs d{};
   d.rhs = rhs;
@@ -580,6 +596,27 @@ int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
   d.us = fs[0]; d.vs = fs[1]; d.ws = fs[2];
   d.cdx = 1.0 / (h->dx * c.dt); d.cdy = 1.0 / (h->dy * c.dt); d.cdz = 1.0 / (h->dz * c.dt);
   d.one = 1.0; d.mzero = -0.0;
+  return d;
+}
+
+CorrectArgs correct_args(ns_handle* h) {
+  const ns_config& c = h->cfg;
+  CorrectArgs ca{};
+  ca.L = h->L;
+  const double* fs[3];
+  final_star(h, fs);
+  ca.us = fs[0]; ca.vs = fs[1]; ca.ws = fs[2]; ca.dp = h->dp;
+  ca.u = h->u; ca.v = h->v; ca.w = h->w; ca.p = h->p;
+  ca.gx = -c.dt / h->dx; ca.gy = -c.dt / h->dy; ca.gz = -c.dt / h->dz;
+  ca.dp_flag = c.dp_flag; ca.gauge = c.gauge;
+  for (int q = 0; q < 3; ++q) ca.per[q] = c.bc[q] == 1;
+  ca.one = 1.0; ca.mzero = -0.0;
+  return ca;
+}
+
+int enqueue_poisson(ns_handle* h, const double* rhs = nullptr) {
+  const ns_config& c = h->cfg;
+  const DivArgs d = div_args(h, rhs);
   NS_CUDA(h, launch_fft_poisson(h->plan, d, h->spec, h->dp, h->L, h->stream, marker(h)));
   NS_CUDA(h, launch_pr_bc(h->L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, h->dz, h->stream));
   mark(h, "pr_bc", 3);
@@ -599,7 +636,9 @@ int enqueue_step(ns_handle* h, bool first, cudaEvent_t after_predict = nullptr) 
   return enqueue_tail(h, false);
 }
 
-int enqueue_tail(ns_handle* h, bool adi_xy_done) {
+// The viscous part after the predictor: the ADI sweeps (x and y unless
+// already done plane by plane) or the velocity BC fill.
+int enqueue_viscous(ns_handle* h, bool adi_xy_done) {
   const ns_config& c = h->cfg;
   if (c.scheme == NS_AB2_CN) {
     for (int ax = adi_xy_done ? 2 : 0; ax < 3; ++ax) {
@@ -610,20 +649,87 @@ int enqueue_tail(ns_handle* h, bool adi_xy_done) {
     NS_CUDA(h, launch_vel_bc(h->L, h->us, h->vs, h->ws, h->faces[0], c.bc, h->stream));
     mark(h, "vel_bc", 3);
   }
-  int s = enqueue_poisson(h);
+  return NS_OK;
+}
+
+int enqueue_tail(ns_handle* h, bool adi_xy_done) {
+  int s = enqueue_viscous(h, adi_xy_done);
   if (s) return s;
-  CorrectArgs ca{};
-  ca.L = h->L;
-  const double* fs[3];
-  final_star(h, fs);
-  ca.us = fs[0]; ca.vs = fs[1]; ca.ws = fs[2]; ca.dp = h->dp;
-  ca.u = h->u; ca.v = h->v; ca.w = h->w; ca.p = h->p;
-  ca.gx = -c.dt / h->dx; ca.gy = -c.dt / h->dy; ca.gz = -c.dt / h->dz;
-  ca.dp_flag = c.dp_flag; ca.gauge = c.gauge;
-  for (int q = 0; q < 3; ++q) ca.per[q] = c.bc[q] == 1;
-  ca.one = 1.0; ca.mzero = -0.0;
-  NS_CUDA(h, launch_correct(ca, h->stream));
+  s = enqueue_poisson(h);
+  if (s) return s;
+  NS_CUDA(h, launch_correct(correct_args(h), h->stream));
   mark(h, "correct");
+  return NS_OK;
+}
+
+// Out-copy of the slots [k0, k1) along z of field fid (0..2 u/v/w-type, 3
+// p-type) into the host array dst: gathered on the compute stream into the
+// staging buffer (at the array's own offsets; zero_hist zeroes the history's
+// entries outside its interior ranges), then copied on the copy stream, which
+// thus carries nothing but copies.
+cudaError_t out_planes(ns_handle* h, const double* field, double* dst, int fid, int k0, int k1, double* stage,
+                       bool zero_hist, cudaEvent_t ev) {
+  const ns_config& c = h->cfg;
+  const int off = fid == 2 ? 1 : 0;  // w-type: slot k is reference plane k - 1
+  const int r0 = std::max(k0 - off, 0), r1 = std::min(k1 - off, ext_of(c, fid, 2));
+  if (r1 <= r0) return cudaSuccess;
+  int lo[3], hi[3];
+  hist_range(c, fid, lo, hi);
+  cudaError_t e = pack_launch(h, const_cast<double*>(field), stage, fid, false, zero_hist ? lo : nullptr,
+                              zero_hist ? hi : nullptr, h->stream, r0, r1);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaEventRecord(ev, h->stream)) != cudaSuccess) return e;
+  if ((e = cudaStreamWaitEvent(h->xfer, ev, 0)) != cudaSuccess) return e;
+  const size_t pd = (size_t)ext_of(c, fid, 0) * ext_of(c, fid, 1);
+  return cudaMemcpyAsync(dst + pd * r0, stage + pd * r0, sizeof(double) * pd * (r1 - r0), cudaMemcpyDeviceToHost,
+                         h->xfer);
+}
+
+// The tail of ns_step_host in z-slabs (plans whose inverse passes work plane
+// by plane), after the viscous part.  The forward passes and the line solve
+// cover the whole box.  Then the inverse passes, the pressure ghosts and the
+// correction run slab by slab [tb[s], tb[s+1]) (slots), and each slab's u, v,
+// w, p are gathered and copied out on the copy stream while the next slab is
+// computed.  Cell planes nz-1 and nz come first: slot 0 of the face fields
+// (its periodic image) and the gauge corner dp(0,0,0) read them.  The z pass
+// of the ghost fill runs with slab 0, once planes 1 and nz are final.  Every
+// value is computed by the same kernels from the same inputs as in
+// enqueue_tail, so the result has the same bits.
+int step_host_slab_tail(ns_handle* h, const std::vector<int>& tb, double* uo, double* vo, double* wo, double* po,
+                        int ev0) {
+  const ns_config& c = h->cfg;
+  const Layout& L = h->L;
+  const int nz = c.nz;
+  const DivArgs d = div_args(h, nullptr);
+  NS_CUDA(h, launch_poisson_fwd(h->plan, d, h->spec, h->dp, L, h->stream, marker(h)));
+  trace_mark(h, h->stream, "poisson fwd");
+  const CorrectArgs ca = correct_args(h);
+  const int top = std::max(1, nz - 1);
+  NS_CUDA(h, launch_poisson_inv(h->plan, d, h->spec, h->dp, L, h->stream, marker(h), top, nz + 1));
+  NS_CUDA(h, launch_pr_bc_planes(L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, top, nz + 1, h->stream));
+  mark(h, "pr_bc", 2);
+  double* want[4] = {uo, vo, wo, po};
+  const double* have[4] = {h->u, h->v, h->w, h->p};
+  const int ntail = (int)tb.size() - 1;
+  for (int s = 0; s < ntail; ++s) {
+    const int lo = tb[s], hi = tb[s + 1];
+    const int k0 = std::max(lo, 1), k1 = std::min(hi, top);
+    if (k1 > k0) {
+      NS_CUDA(h, launch_poisson_inv(h->plan, d, h->spec, h->dp, L, h->stream, marker(h), k0, k1));
+      NS_CUDA(h, launch_pr_bc_planes(L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, k0, k1, h->stream));
+      mark(h, "pr_bc", 2);
+    }
+    if (s == 0) {
+      NS_CUDA(h, launch_pr_bc_z(L, h->dp, h->faces[0], c.pbc[2], h->dz, h->stream));
+      mark(h, "pr_bc");
+    }
+    NS_CUDA(h, launch_correct_planes(ca, lo, hi, h->stream));
+    mark(h, "correct");
+    trace_mark(h, h->stream, "tail slab", s, lo, hi);
+    for (int q = 0; q < 4; ++q)
+      if (want[q]) NS_CUDA(h, out_planes(h, have[q], want[q], q, lo, hi, h->stage_f[q], false, h->ev_slab[ev0 + 4 * s + q]));
+    trace_mark(h, h->xfer, "d2h slab", s, lo, hi);
+  }
   return NS_OK;
 }
 
@@ -820,6 +926,7 @@ void free_all(ns_handle* h) {
   if (h->stage) cudaFree(h->stage);
   if (h->stage2) cudaFree(h->stage2);
   if (h->xfer) cudaStreamDestroy(h->xfer);
+  if (h->side) cudaStreamDestroy(h->side);
   for (int b = 0; b < 2; ++b) {
     if (h->ev_full[b]) cudaEventDestroy(h->ev_full[b]);
     if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
@@ -828,6 +935,7 @@ void free_all(ns_handle* h) {
   for (double* b : h->stage_f)
     if (b) cudaFree(b);
   for (cudaEvent_t e : h->ev_slab) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->trace_pool) cudaEventDestroy(e);
   if (h->tw) cudaFree(h->tw);
   if (h->diag_bits) cudaFree(h->diag_bits);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -896,6 +1004,7 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
   }
   ns_handle* h = new ns_handle();
   h->cfg = *cfg;
+  h->trace = std::getenv("NS_TRACE") != nullptr;
   h->L = make_layout(cfg->nx, cfg->ny, cfg->nz);
   h->dx = cfg->lx / cfg->nx; h->dy = cfg->ly / cfg->ny; h->dz = cfg->lz / cfg->nz;
   auto bail = [&](int code) { free_all(h); delete h; return code; };
@@ -1006,15 +1115,53 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   std::vector<In> in = {{h->u, u, 0, 0}, {h->v, v, 1, 1}, {h->w, w, 2, 2}};
   if (hist) { in.push_back({h->hx, hx, 0, 4}); in.push_back({h->hy, hy, 1, 5}); in.push_back({h->hz, hz, 2, 6}); }
   if (c.dp_flag) in.push_back({h->p, p, 3, 3});
-  for (const In& f : in)
-    if (!h->stage_f[f.q]) NS_CUDA(h, cudaMalloc(&h->stage_f[f.q], field_bytes(c, f.fid)));
-  // z-slabs of 4 predictor chunks: copy, scatter, predict, x and y sweeps of
-  // slab s run while slab s+1 is being copied.  (Slabs of 2 chunks left each
-  // predictor launch under one wave of CTAs, and the compute of a slab
-  // outlasted its copy.)
+  // state out; staging buffer q serves field q in and out (disjoint planes at any time)
+  double* const out[7] = {uo, vo, wo, po, hxo, hyo, hzo};
+  const double* const out_dev[7] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz};
+  bool need_stage[7] = {false, false, false, false, false, false, false};
+  for (const In& f : in) need_stage[f.q] = true;
+  for (int q = 0; q < 7; ++q) need_stage[q] = need_stage[q] || out[q];
+  for (int q = 0; q < 7; ++q)
+    if (need_stage[q] && !h->stage_f[q]) NS_CUDA(h, cudaMalloc(&h->stage_f[q], field_bytes(c, q < 4 ? q : q - 4)));
+  // z-slabs: copy, scatter, predict, x and y sweeps of slab s run while slab
+  // s+1 is being copied.  The first slab holds one predictor chunk (and the
+  // two planes above it that the predictor reads), so compute starts early;
+  // then 4 chunks a slab (2-chunk slabs left each launch under one wave of
+  // CTAs); the compute of the last slab is not hidden, so the slabs shrink
+  // towards the top: half the rest (whole chunks) once less than two full
+  // slabs remain.
   const int KC = predict_chunk_planes();
-  const int S = 4 * KC, nslab = (nz + 2 + S - 1) / S;
-  while ((int)h->ev_slab.size() < nslab + 1) {
+  const int S = 4 * KC;
+  std::vector<int> fb = {0, std::min(nz + 2, KC + 2)};
+  while (fb.back() < nz + 2) {
+    const int r = nz + 2 - fb.back();
+    int take = r;
+    if (r >= 2 * S) take = S;
+    else if (r > KC + 2) take = std::max(KC, (r / 2 + KC - 1) / KC * KC);
+    fb.push_back(fb.back() + take);
+  }
+  const int nslab = (int)fb.size() - 1;
+  // The tail in z-slabs as well when the inverse passes work plane by plane:
+  // each slab's u, v, w, p leave while the next slab is computed.  The first
+  // slab is small (its compute comes before any of the tail's copies).
+  const bool slab_tail = poisson_inv_by_planes(h->plan);
+  std::vector<int> tb = {0};
+  if (slab_tail) {
+    // sizes doubling from KC/2 + 1 up to S: each slab's compute about as
+    // long as the copy of the one before
+    int sz = KC / 2 + 1;
+    while (tb.back() < nz + 2) {
+      tb.push_back(std::min(nz + 2, tb.back() + sz));
+      sz = std::min(S, tb.size() == 2 ? KC : 2 * sz);
+    }
+  }
+  while (tb.back() < nz + 2) tb.push_back(std::min(nz + 2, tb.back() + S));
+  const int ntail = (int)tb.size() - 1;
+  // events: front slabs (copy done), start, history out (3 per front slab),
+  // state out (4 per tail slab), predictor done (per front slab), sweeps done
+  const int ev_start = nslab, ev_hist = nslab + 1, ev_tail = ev_hist + 3 * nslab, ev_pred = ev_tail + 4 * ntail;
+  const int ev_sweeps = ev_pred + nslab;
+  while ((int)h->ev_slab.size() < ev_sweeps + 1) {
     cudaEvent_t e;
     NS_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     h->ev_slab.push_back(e);
@@ -1024,8 +1171,9 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     NS_CUDA(h, cudaMemsetAsync(h->hy, 0, L.fsize * sizeof(double), h->stream));
     NS_CUDA(h, cudaMemsetAsync(h->hz, 0, L.fsize * sizeof(double), h->stream));
   }
-  NS_CUDA(h, cudaEventRecord(h->ev_slab[nslab], h->stream));
-  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[nslab], 0));
+  trace_mark(h, h->stream, "start");
+  NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_start], h->stream));
+  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[ev_start], 0));
   auto plane_bytes = [&](int fid) {
     return sizeof(double) * (size_t)ext_of(c, fid, 0) * ext_of(c, fid, 1);
   };
@@ -1054,21 +1202,21 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     NS_CUDA(h, launch_extra_slots(L, h->u, h->v, h->w, zonly, h->stream));
   }
   for (int s = 0; s < nslab; ++s) {
-    const int lo = s * S, hi = std::min(nz + 2, (s + 1) * S);
+    const int lo = fb[s], hi = fb[s + 1];
     for (const In& f : in) {
       int r0, r1;
       ref_range(f, lo, hi, r0, r1);
       NS_CUDA(h, copy_in(f, r0, r1));
     }
     NS_CUDA(h, cudaEventRecord(h->ev_slab[s], h->xfer));
+    trace_mark(h, h->xfer, "h2d slab", s, lo, hi);
   }
   const bool cn = c.scheme == NS_AB2_CN;
   const bool first = !hist && c.scheme != NS_EULER;
-  const int nch = (nz + KC - 1) / KC;
-  int c_next = 0, xy_done = 0;
+  int pred_done = 1, xy_done = 0, hist_done = 0;  // next cell plane to predict; slots swept / sent out
   PredictArgs pa = predict_args(h);
   for (int s = 0; s < nslab; ++s) {
-    const int lo = s * S, hi = std::min(nz + 2, (s + 1) * S);
+    const int lo = fb[s], hi = fb[s + 1];
     NS_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_slab[s], 0));
     for (const In& f : in) {
       int r0, r1;
@@ -1081,64 +1229,66 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
           L, h->u, h->v, c.bc[0] == 1, c.bc[1] == 1, lo, hi);
       NS_CUDA(h, cudaGetLastError());
     }
-    // chunks whose planes (and the two planes above, read by the prefetch) have arrived
-    int c_ready = c_next;
-    while (c_ready < nch) {
-      const int k1 = std::min(1 + KC * (c_ready + 1), nz + 1);
-      if (std::min(k1 + 2, nz + 2) > hi) break;
-      ++c_ready;
-    }
-    if (c_ready > c_next) {
-      NS_CUDA(h, launch_predict_range(pa, c.scheme, first, c.dp_flag != 0, c_next, c_ready, h->stream));
+    trace_mark(h, h->stream, "scatter", s, lo, hi);
+    // cell planes whose stencil and the two planes above it (read by the
+    // prefetch) have arrived; a quarter of the range per CTA, at most
+    // KC planes: short ranges at the top spread over as many CTAs as a
+    // full slab, so the compute left after the last copy is short.
+    const int e = hi >= nz + 2 ? nz + 1 : std::min(nz + 1, hi - 2);
+    if (e > pred_done) {
+      const int kc = std::max(2, std::min(KC, (e - pred_done) / 4));
+      NS_CUDA(h, launch_predict_planes(pa, c.scheme, first, c.dp_flag != 0, pred_done, e, kc, h->stream));
       mark(h, "predict");
-      c_next = c_ready;
-      if (cn) {  // x and y sweeps of the planes the predictor has finished
-        const int zhi = c_ready == nch ? nz + 2 : 1 + KC * c_ready;
+      trace_mark(h, h->stream, "predict", s, lo, hi);
+      pred_done = e;
+      // the history of the finished planes is final: out on the copy stream
+      // (after the copies in, in stream order)
+      const int done = e == nz + 1 ? nz + 2 : e;
+      for (int q = 0; q < 3; ++q)
+        if (out[4 + q])
+          NS_CUDA(h, out_planes(h, out_dev[4 + q], out[4 + q], q, hist_done, done, h->stage_f[4 + q], true,
+                                h->ev_slab[ev_hist + 3 * s + q]));
+      hist_done = done;
+      if (cn) {
+        // x and y sweeps of the planes the predictor has finished, on the
+        // side stream: they touch only those planes of u*, v*, w* (and their
+        // second buffers), which the next predictor launch neither reads nor
+        // writes, so they fill the wave tails of the next slab's launches.
+        NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_pred + s], h->stream));
+        NS_CUDA(h, cudaStreamWaitEvent(h->side, h->ev_slab[ev_pred + s], 0));
         for (int ax = 0; ax < 2; ++ax) {
           AdiArgs a = adi_args(h, ax);
           a.z0 = xy_done;
-          a.z1 = zhi;
-          NS_CUDA(h, launch_adi(ax, a, h->stream));
+          a.z1 = done;
+          NS_CUDA(h, launch_adi(ax, a, h->side));
           mark(h, ax == 0 ? "adi_x" : "adi_y");
+          trace_mark(h, h->side, ax == 0 ? "adi_x" : "adi_y", s, lo, hi);
         }
-        xy_done = zhi;
+        xy_done = done;
       }
     }
   }
-  if (c_next != nch) return fail(h, NS_ERR_ARG, "internal: predictor chunks left after the last slab");
-  NS_CUDA(h, cudaEventRecord(h->ev_aux[0], h->stream));  // the history is final
-  int st = enqueue_tail(h, cn);
-  if (st) return st;
-  NS_CUDA(h, cudaEventRecord(h->ev_aux[1], h->stream));
-  // state out on the copy stream: the history while the rest of the step runs
-  int nb = 0;
-  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_aux[0], 0));
-  {
-    double* od[3];
-    const double* os[3];
-    int of[3];
-    bool oz[3];
-    int m = 0;
-    double* want[3] = {hxo, hyo, hzo};
-    const double* have[3] = {h->hx, h->hy, h->hz};
-    for (int q = 0; q < 3; ++q)
-      if (want[q]) { od[m] = want[q]; os[m] = have[q]; of[m] = q; oz[m] = true; ++m; }
-    NS_CUDA(h, d2h_on_xfer(h, m, od, os, of, oz, nb));
+  if (pred_done != nz + 1) return fail(h, NS_ERR_ARG, "internal: predictor planes left after the last slab");
+  if (cn) {
+    NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_sweeps], h->side));
+    NS_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_slab[ev_sweeps], 0));
   }
-  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_aux[1], 0));
-  {
-    double* od[4];
-    const double* os[4];
-    int of[4];
-    int m = 0;
-    double* want[4] = {uo, vo, wo, po};
-    const double* have[4] = {h->u, h->v, h->w, h->p};
+  if (hxo || hyo || hzo) trace_mark(h, h->xfer, "d2h history");
+  int st = slab_tail ? enqueue_viscous(h, cn) : enqueue_tail(h, cn);
+  if (st) return st;
+  trace_mark(h, h->stream, slab_tail ? "viscous" : "tail");
+  if (slab_tail) {
+    st = step_host_slab_tail(h, tb, uo, vo, wo, po, ev_tail);
+    if (st) return st;
+  } else {
     for (int q = 0; q < 4; ++q)
-      if (want[q]) { od[m] = want[q]; os[m] = have[q]; of[m] = q; ++m; }
-    NS_CUDA(h, d2h_on_xfer(h, m, od, os, of, nullptr, nb));
+      if (out[q])
+        NS_CUDA(h, out_planes(h, out_dev[q], out[q], q, 0, nz + 2, h->stage_f[q], false, h->ev_slab[ev_tail + q]));
+    trace_mark(h, h->xfer, "d2h state");
   }
   NS_CUDA(h, cudaStreamSynchronize(h->xfer));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  trace_flush(h);
   h->first_pending = false;
   h->steps = 1;
   return NS_OK;

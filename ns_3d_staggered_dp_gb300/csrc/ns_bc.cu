@@ -107,9 +107,11 @@ __device__ __forceinline__ void pr_bc_body(const Layout& L, double* dp, const Fa
   }
 }
 
+// Lines t in [t0, t1) of the pass along AXIS.
 template <int AXIS>
-__global__ void pr_bc_kernel(Layout L, double* dp, FacePlanes F, int pbc, double h) {
-  pr_bc_body<AXIS>(L, dp, F, pbc, h, blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void pr_bc_kernel(Layout L, double* dp, FacePlanes F, int pbc, double h, int t0, int t1) {
+  const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < t1) pr_bc_body<AXIS>(L, dp, F, pbc, h, t);
 }
 
 // Batched fill pass along AXIS: velocity (PR false) or pressure ghosts, one
@@ -188,10 +190,27 @@ cudaError_t launch_pr_bc(const Layout& L, double* dp, const FaceSet& F, const in
   for (int a = 0; a < 3; ++a) {
     const int n = plane_count(L, a);
     dim3 grid((n + 255) / 256);
-    if (a == 0) pr_bc_kernel<0><<<grid, 256, 0, st>>>(L, dp, F.ax[0], pbc[0], h[0]);
-    if (a == 1) pr_bc_kernel<1><<<grid, 256, 0, st>>>(L, dp, F.ax[1], pbc[1], h[1]);
-    if (a == 2) pr_bc_kernel<2><<<grid, 256, 0, st>>>(L, dp, F.ax[2], pbc[2], h[2]);
+    if (a == 0) pr_bc_kernel<0><<<grid, 256, 0, st>>>(L, dp, F.ax[0], pbc[0], h[0], 0, n);
+    if (a == 1) pr_bc_kernel<1><<<grid, 256, 0, st>>>(L, dp, F.ax[1], pbc[1], h[1], 0, n);
+    if (a == 2) pr_bc_kernel<2><<<grid, 256, 0, st>>>(L, dp, F.ax[2], pbc[2], h[2], 0, n);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pr_bc_planes(const Layout& L, double* dp, const FaceSet& F, const int pbc[3], double dx,
+                                double dy, int k0, int k1, cudaStream_t st) {
+  if (k0 < 0 || k1 > L.nz + 2 || k0 > k1) return cudaErrorInvalidValue;
+  if (k0 == k1) return cudaSuccess;
+  // a line of the x pass is (j, k) with t = j + (ny+2) k, of the y pass (i, k) with t = i + (nx+2) k
+  const int px = L.ny + 2, py = L.nx + 2;
+  pr_bc_kernel<0><<<(px * (k1 - k0) + 255) / 256, 256, 0, st>>>(L, dp, F.ax[0], pbc[0], dx, px * k0, px * k1);
+  pr_bc_kernel<1><<<(py * (k1 - k0) + 255) / 256, 256, 0, st>>>(L, dp, F.ax[1], pbc[1], dy, py * k0, py * k1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pr_bc_z(const Layout& L, double* dp, const FaceSet& F, int pbc_z, double dz, cudaStream_t st) {
+  const int n = plane_count(L, 2);
+  pr_bc_kernel<2><<<(n + 255) / 256, 256, 0, st>>>(L, dp, F.ax[2], pbc_z, dz, 0, n);
   return cudaGetLastError();
 }
 

@@ -60,8 +60,10 @@ __device__ __forceinline__ void correct_body(const CorrectArgs& a, long long t) 
   }
 }
 
-__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a) {
-  correct_body(a, blockIdx.x * (long long)blockDim.x + threadIdx.x);
+// Slots t in [t0, t1) of the padded box (x fastest).
+__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a, long long t0, long long t1) {
+  const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < t1) correct_body(a, t);
 }
 
 // Batched: one 256-element chunk of a subdomain box per work item.
@@ -82,9 +84,14 @@ cudaError_t launch_correct_batch(const CorrectArgs* tab, const BatchItem* items,
   return cudaGetLastError();
 }
 
-cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st) {
-  const long long tot = (long long)(a.L.nx + 2) * (a.L.ny + 2) * (a.L.nz + 2);
-  correct_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a);
+cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st) { return launch_correct_planes(a, 0, a.L.nz + 2, st); }
+
+cudaError_t launch_correct_planes(const CorrectArgs& a, int k0, int k1, cudaStream_t st) {
+  if (k0 < 0 || k1 > a.L.nz + 2 || k0 > k1) return cudaErrorInvalidValue;
+  if (k0 == k1) return cudaSuccess;
+  const long long plane = (long long)(a.L.nx + 2) * (a.L.ny + 2);
+  const long long n = plane * (k1 - k0);
+  correct_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, plane * k0, plane * k1);
   return cudaGetLastError();
 }
 

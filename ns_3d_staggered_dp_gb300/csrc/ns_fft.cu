@@ -225,29 +225,30 @@ struct YZ {
   }
 };
 
-// Line geometry of a y/z-pass block.  Blocks with blockIdx.x < nxh/LPC own
-// LPC consecutive kx at one outer index; the last column of blocks owns the
+// Line geometry of a y/z-pass block over the outer indices [o0, o1) (kz for
+// a y pass, ky for a z pass).  Blocks with blockIdx.x < nxh/LPC own LPC
+// consecutive kx at one outer index; the last column of blocks owns the
 // Nyquist plane kx = nx/2, with lanes over LPC consecutive outer indices.
 struct LineGeo {
   long long base;
   bool valid;
 };
 __host__ __device__ __forceinline__ int yz_nblk(int nxh, int LPC) { return (nxh - 1 + LPC - 1) / LPC; }
-__device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, int l, int LPC) {
+__device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int l, int LPC, int o0, int o1) {
   const int M = nxh - 1;
   const int nblk = yz_nblk(nxh, LPC);
   LineGeo G;
   int kx, o;
   if ((int)blockIdx.x < nblk) {
     kx = blockIdx.x * LPC + l;
-    o = blockIdx.y;
+    o = o0 + blockIdx.y;
     G.valid = kx < M;
     if (!G.valid) kx = 0;
   } else {
     kx = M;
-    o = blockIdx.y * LPC + l;
-    G.valid = o < (axis == 1 ? nz : ny);
-    if (!G.valid) o = 0;
+    o = o0 + blockIdx.y * LPC + l;
+    G.valid = o < o1;
+    if (!G.valid) o = o0;
   }
   if (axis == 1) G.base = kx + (long long)nxh * ny * o;  // line along y at (kx, kz = o)
   else G.base = kx + (long long)nxh * o;                 // line along z at (kx, ky = o)
@@ -256,15 +257,15 @@ __device__ __forceinline__ LineGeo yz_line(int axis, int nxh, int ny, int nz, in
 
 // Complex FFT along y (AXIS 1) or z (AXIS 2), forward (DIR -1) or inverse.
 template <int AXIS, int N, int DIR>
-__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_yz_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_yz_kernel(FftPlan P, double2* __restrict__ spec, FOne c,
+                                                                          int o0, int o1) {
   using F = YZ<N>;
   constexpr int LPC = F::LPC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2* sb = reinterpret_cast<double2*>(smem_raw);
   const int l = threadIdx.x, t = threadIdx.y;
-  const LineGeo G = yz_line(AXIS, P.nxh, P.ny, P.nz, l, LPC);
-  const int n_other = AXIS == 1 ? P.nz : P.ny;
-  if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && blockIdx.y * LPC >= (unsigned)n_other) return;  // whole block idle
+  const LineGeo G = yz_line(AXIS, P.nxh, P.ny, l, LPC, o0, o1);
+  if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && (int)(blockIdx.y * LPC) >= o1 - o0) return;  // whole block idle
   double2* g = spec + G.base;
   const long long st = AXIS == 1 ? (long long)P.nxh : (long long)P.nxh * P.ny;
   const double2* tw = AXIS == 1 ? P.tw_y : P.tw_z;
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_z_solve_kernel(Ff
   double2* sb = reinterpret_cast<double2*>(smem_raw);
   const int l = threadIdx.x, t = threadIdx.y;
   if ((int)blockIdx.x == yz_nblk(P.nxh, LPC) && blockIdx.y * LPC >= (unsigned)P.ny) return;
-  const LineGeo G = yz_line(2, P.nxh, P.ny, P.nz, l, LPC);
+  const LineGeo G = yz_line(2, P.nxh, P.ny, l, LPC, 0, P.ny);
   double2* g = spec + G.base;
   const double* lam = P.inv_lam + G.base;
   const long long st = (long long)P.nxh * P.ny;
@@ -434,14 +435,14 @@ __global__ void __launch_bounds__(256) fft_x_fwd_kernel(FftPlan P, DivArgs d, do
 
 template <int M, bool ALIGNED>
 __global__ void __launch_bounds__(256) fft_x_inv_kernel(FftPlan P, const double2* __restrict__ spec, double* dp,
-                                                        Layout L, FOne c) {
+                                                        Layout L, FOne c, int line0, int line1) {
   using X = XP<M>;
   constexpr int R1 = X::R1, R2 = X::R2, T = X::T, KQ = X::KQ;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = threadIdx.x, l = threadIdx.y;
-  const int line = blockIdx.x * X::LINES + l;
-  const int ny = L.ny, nz = L.nz;
-  const bool valid = line < ny * nz;
+  const int line = line0 + blockIdx.x * X::LINES + l;
+  const int ny = L.ny;
+  const bool valid = line < line1;
   const int j = valid ? 1 + line % ny : 1;
   const int k = valid ? 1 + line / ny : 1;
   double2* sb = reinterpret_cast<double2*>(smem_raw) + (long long)l * X::LS;
@@ -521,27 +522,31 @@ cudaError_t launch_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cuda
   kern<<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, d, spec);
   return cudaGetLastError();
 }
+// x lines of the cell planes k in [k0, k1) (slots 1..nz).
 template <int M>
-cudaError_t launch_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, FOne c, cudaStream_t st) {
+cudaError_t launch_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, FOne c, cudaStream_t st,
+                         int k0, int k1) {
   const size_t sm = xp_smem<M>();
   auto kern = P.dp_unaligned ? fft_x_inv_kernel<M, false> : fft_x_inv_kernel<M, true>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  const int lines = L.ny * L.nz;
+  const int line0 = L.ny * (k0 - 1), line1 = L.ny * (k1 - 1);
   dim3 block(XP<M>::T, XP<M>::LINES);
-  kern<<<(lines + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, spec, dp, L, c);
+  kern<<<(line1 - line0 + XP<M>::LINES - 1) / XP<M>::LINES, block, sm, st>>>(P, spec, dp, L, c, line0, line1);
   return cudaGetLastError();
 }
+// Lines of the outer indices [o0, o1) (o1 < 0: all of them).
 template <int AXIS, int N, int DIR>
-cudaError_t launch_yz(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
+cudaError_t launch_yz(const FftPlan& P, double2* spec, FOne c, cudaStream_t st, int o0 = 0, int o1 = -1) {
   const size_t sm = yz_smem<N>();
   auto kern = fft_yz_kernel<AXIS, N, DIR>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
+  if (o1 < 0) o1 = AXIS == 1 ? P.nz : P.ny;
   constexpr int LPC = lpc<N>();
-  dim3 grid(yz_nblk(P.nxh, LPC) + 1, AXIS == 1 ? P.nz : P.ny);
+  dim3 grid(yz_nblk(P.nxh, LPC) + 1, o1 - o0);
   dim3 block(LPC, Split<N>::R1);
-  kern<<<grid, block, sm, st>>>(P, spec, c);
+  kern<<<grid, block, sm, st>>>(P, spec, c, o0, o1);
   return cudaGetLastError();
 }
 template <int N>
@@ -600,7 +605,9 @@ cudaError_t launch_fft_forward3(const FftPlan& P, const DivArgs& d, double2* spe
   return e;
 }
 
-cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+// Divergence, forward transforms and the line solve: everything up to the
+// inverse passes.
+cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk) {
   const FOne c{d.one, d.mzero};
   cudaError_t e = cudaSuccess;
@@ -645,9 +652,27 @@ cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec
     if ((e = launch_tri_solve(3 - m, P, spec, st)) != cudaSuccess) return e;
     mk(m == 1 ? "tri_z_solve" : "tri_y_solve");
   }
+  return e;
+}
+
+bool poisson_inv_by_planes(const FftPlan& P) { return P.kind[0] == 0 && P.kind[1] == 0; }
+
+// The inverse passes into dp.  With poisson_inv_by_planes(P) both passes
+// work plane by plane in z, and [k0, k1) (cell slots 1..nz) selects planes;
+// otherwise the range must be all of [1, nz + 1).
+cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk, int k0, int k1) {
+  const FOne c{d.one, d.mzero};
+  cudaError_t e = cudaSuccess;
+  if (k0 < 1 || k1 > L.nz + 1 || k0 > k1) return cudaErrorInvalidValue;
+  if (k0 == k1) return cudaSuccess;
+  const bool part = k0 != 1 || k1 != L.nz + 1;
+  if (part && !poisson_inv_by_planes(P)) return cudaErrorInvalidValue;
+  const int m = P.kind[1] == 2 ? 2 : 1;
+  const int nm = m == 1 ? P.ny : P.nz;
   if (P.kind[m] == 0) {
     if (m == 1) {
-#define Y_INV(n) e = launch_yz<1, (n), 1>(P, spec, c, st)
+#define Y_INV(n) e = launch_yz<1, (n), 1>(P, spec, c, st, k0 - 1, k1 - 1)
       NS_SIZE_SWITCH(nm, Y_INV)
 #undef Y_INV
     } else {
@@ -662,7 +687,7 @@ cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec
     mk(m == 1 ? "dense_y_inv" : "dense_z_inv");
   }
   if (P.kind[0] == 0) {
-#define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st)
+#define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st, k0, k1)
     NS_SIZE_SWITCH(P.nx, X_INV)
 #undef X_INV
     if (e != cudaSuccess) return e;
@@ -672,6 +697,13 @@ cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec
     mk("dense_x_inv");
   }
   return e;
+}
+
+cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk) {
+  cudaError_t e = launch_poisson_fwd(P, d, spec, dp, L, st, mk);
+  if (e != cudaSuccess) return e;
+  return launch_poisson_inv(P, d, spec, dp, L, st, mk, 1, L.nz + 1);
 }
 
 }  // namespace ns

@@ -48,7 +48,9 @@ struct PredictArgs {
   double dt, e1, e2;  // AB2: u* = u + e1*rhs + e2*prev
   double gpx, gpy, gpz;  // -dt/dx etc. (dp_flag)
   double ix2, iy2, iz2, lap0;  // diffusion-only mode
-  int bz0;                     // first z-chunk of the launch (chunk ranges of the pipelined host step)
+  // Plane ranges with their own chunk depth (0: the defaults): chunk bz holds
+  // the planes 1 + koff + kc*bz .. up to kend (exclusive; 0: nz + 1).
+  int kc, koff, kend;
 };
 
 // Combine the stencil pieces into u* and rewrite the AB2 history at g.
@@ -84,9 +86,12 @@ __device__ __forceinline__ double predictor_combine(const PredictArgs& a, const 
 
 size_t predict_smem_bytes();
 cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st);
-// The predictor on z-chunks [c0, c1) only (chunks of predict_chunk_planes() planes from slot 1).
-cudaError_t launch_predict_range(PredictArgs a, int scheme, bool first, bool dpf, int c0, int c1, cudaStream_t st);
 int predict_chunk_planes();
+// The predictor on the cell planes [p0, p1) (1 <= p0 < p1 <= nz + 1) in
+// chunks of kc planes per CTA: small chunks spread a short range over more
+// CTAs (less latency, a little more work per plane).
+cudaError_t launch_predict_planes(PredictArgs a, int scheme, bool first, bool dpf, int p0, int p1, int kc,
+                                  cudaStream_t st);
 // Predictor tiles of one box (work items of the batched launch).
 void predict_tiles(const Layout& L, int& gx, int& gy, int& gz);
 // Batched predictor over the items (grid <= 0: one wave of resident CTAs).
@@ -114,6 +119,14 @@ cudaError_t launch_extra_slots(const Layout& L, double* u, double* v, double* w,
 // pr_bc_staggered (NS_functions.f90:1403-1464), the three axis passes.
 cudaError_t launch_pr_bc(const Layout& L, double* dp, const FaceSet& F, const int pbc[3], double dx, double dy,
                          double dz, cudaStream_t st);
+// The same fill in parts: the x and y passes over the planes z in [k0, k1),
+// and (z_pass) the z pass, which writes both ghost planes from planes 1 and
+// nz.  Filling every cell plane 1..nz by x/y parts and then running the z
+// pass gives the bits of launch_pr_bc: its x and y passes over the ghost
+// planes are overwritten by its z pass.
+cudaError_t launch_pr_bc_planes(const Layout& L, double* dp, const FaceSet& F, const int pbc[3], double dx,
+                                double dy, int k0, int k1, cudaStream_t st);
+cudaError_t launch_pr_bc_z(const Layout& L, double* dp, const FaceSet& F, int pbc_z, double dz, cudaStream_t st);
 // Elements of the face plane normal to an axis (ghosts included).
 int plane_count(const Layout& L, int axis);
 // Per-subdomain arguments of the batched fills.
@@ -226,9 +239,18 @@ struct DivArgs {
 // Forward 3D FFT of the cell field d.rhs (all-periodic plan): spec = 2 x DFT.
 cudaError_t launch_fft_forward3(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st,
                                 const Marker& mk);
-// The spectral solve (FFT and dense axes mixed), divergence to dp interior.
+// The spectral solve (FFT and dense axes mixed), divergence to dp interior:
+// launch_poisson_fwd (divergence, forward passes, line solve) followed by
+// launch_poisson_inv over all planes.
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk);
+cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk);
+// True when both inverse passes are FFTs along x and y, which work plane by
+// plane in z: launch_poisson_inv then accepts any cell-plane range [k0, k1).
+bool poisson_inv_by_planes(const FftPlan& P);
+cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk, int k0, int k1);
 // Symmetry bits of a dense transform pair of even size n (sym in FftPlan),
 // checked entry by entry on the host (ns_dct.cu).
 int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double>& G);
@@ -272,6 +294,8 @@ struct CorrectArgs {
   double one, mzero;
 };
 cudaError_t launch_correct(const CorrectArgs& a, cudaStream_t st);
+// The correction of the slot planes z in [k0, k1) only (0 <= k0 <= k1 <= nz + 2).
+cudaError_t launch_correct_planes(const CorrectArgs& a, int k0, int k1, cudaStream_t st);
 // Batched correction over the items (sub, 256-element chunk bx of the box).
 cudaError_t launch_correct_batch(const CorrectArgs* tab, const BatchItem* items, int n_items, int grid,
                                  cudaStream_t st);

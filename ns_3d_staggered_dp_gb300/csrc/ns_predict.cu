@@ -124,8 +124,9 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
   const int wy = threadIdx.y;  // 0..TY
   const int i0 = 1 + TX * bx;
   const int j0 = 1 + TY * by;
-  const int k0 = 1 + KC * bz;
-  const int k1 = min(k0 + KC, L.nz + 1);
+  const int kc = a.kc > 0 ? a.kc : KC;
+  const int k0 = 1 + a.koff + kc * bz;
+  const int k1 = min(k0 + kc, a.kend > 0 ? a.kend : L.nz + 1);
   // smem coordinates of this thread's position: x = i0-1+lane+1 -> xa = lane+1; y = j0-1+wy -> yb = wy
   const int xa = lane + 1;
   const int yb = wy;
@@ -256,7 +257,7 @@ template <int SCHEME, bool FIRST, bool DPF, int MODE>
 __global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   predict_body<SCHEME, FIRST, DPF, MODE>(a, *reinterpret_cast<PredSmem*>(smem_raw), blockIdx.x, blockIdx.y,
-                                         blockIdx.z + a.bz0);
+                                         blockIdx.z);
 }
 
 // Batched: persistent CTAs walk the work items (subdomain, tile) of a batch.
@@ -277,17 +278,14 @@ __global__ void __launch_bounds__(TX*(TY + 1)) predict_batch_kernel(const Predic
 size_t predict_smem_bytes() { return sizeof(PredSmem); }
 
 template <int SCHEME, bool FIRST, bool DPF, int MODE>
-static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st, int c0 = 0, int c1 = -1) {
+static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st) {
   auto kern = predict_kernel<SCHEME, FIRST, DPF, MODE>;
   const size_t sm = sizeof(PredSmem);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  const int nch = (a.L.nz + KC - 1) / KC;
-  if (c1 < 0) c1 = nch;
-  if (c0 < 0 || c1 > nch || c0 >= c1) return c0 == c1 ? cudaSuccess : cudaErrorInvalidValue;
   PredictArgs b = a;
-  b.bz0 = c0;
-  dim3 grid((a.L.nx + TX - 1) / TX, (a.L.ny + TY - 1) / TY, c1 - c0);
+  b.kc = b.koff = b.kend = 0;
+  dim3 grid((a.L.nx + TX - 1) / TX, (a.L.ny + TY - 1) / TY, (a.L.nz + KC - 1) / KC);
   dim3 block(TX, TY + 1);
   kern<<<grid, block, sm, st>>>(b);
   return cudaGetLastError();
@@ -295,13 +293,31 @@ static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st, int c0 = 0, i
 
 int predict_chunk_planes() { return KC; }
 
-cudaError_t launch_predict_range(PredictArgs a, int scheme, bool first, bool dpf, int c0, int c1, cudaStream_t st) {
-#define NS_PRED_RCASE(S, F, D) \
-  if (scheme == S && first == F && dpf == D) return launch_t<S, F, D, 0>(a, st, c0, c1);
-  NS_PRED_RCASE(0, false, false) NS_PRED_RCASE(0, false, true) NS_PRED_RCASE(0, true, false) NS_PRED_RCASE(0, true, true)
-  NS_PRED_RCASE(1, false, false) NS_PRED_RCASE(1, false, true) NS_PRED_RCASE(1, true, false) NS_PRED_RCASE(1, true, true)
-  NS_PRED_RCASE(2, false, false) NS_PRED_RCASE(2, false, true) NS_PRED_RCASE(2, true, false) NS_PRED_RCASE(2, true, true)
-#undef NS_PRED_RCASE
+template <int SCHEME, bool FIRST, bool DPF>
+static cudaError_t launch_planes_t(PredictArgs b, cudaStream_t st, int p0, int p1, int kc) {
+  auto kern = predict_kernel<SCHEME, FIRST, DPF, 0>;
+  const size_t sm = sizeof(PredSmem);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  b.kc = kc;
+  b.koff = p0 - 1;
+  b.kend = p1;
+  dim3 grid((b.L.nx + TX - 1) / TX, (b.L.ny + TY - 1) / TY, (p1 - p0 + kc - 1) / kc);
+  dim3 block(TX, TY + 1);
+  kern<<<grid, block, sm, st>>>(b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_predict_planes(PredictArgs a, int scheme, bool first, bool dpf, int p0, int p1, int kc,
+                                  cudaStream_t st) {
+  if (p0 < 1 || p1 > a.L.nz + 1 || p0 > p1 || kc < 1) return cudaErrorInvalidValue;
+  if (p0 == p1) return cudaSuccess;
+#define NS_PRED_PCASE(S, F, D) \
+  if (scheme == S && first == F && dpf == D) return launch_planes_t<S, F, D>(a, st, p0, p1, kc);
+  NS_PRED_PCASE(0, false, false) NS_PRED_PCASE(0, false, true) NS_PRED_PCASE(0, true, false) NS_PRED_PCASE(0, true, true)
+  NS_PRED_PCASE(1, false, false) NS_PRED_PCASE(1, false, true) NS_PRED_PCASE(1, true, false) NS_PRED_PCASE(1, true, true)
+  NS_PRED_PCASE(2, false, false) NS_PRED_PCASE(2, false, true) NS_PRED_PCASE(2, true, false) NS_PRED_PCASE(2, true, true)
+#undef NS_PRED_PCASE
   return cudaErrorInvalidValue;
 }
 

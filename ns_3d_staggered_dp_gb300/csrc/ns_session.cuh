@@ -29,6 +29,7 @@ struct ns_handle {
   double* stage = nullptr;   // host<->device staging of one reference-shaped field
   double* stage2 = nullptr;  // second staging buffer (multi-field transfers)
   cudaStream_t xfer = nullptr;  // copy stream of the multi-field transfers
+  cudaStream_t side = nullptr;  // second compute stream of ns_step_host (x and y sweeps of a slab)
   cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   cudaEvent_t ev_aux[2] = {nullptr, nullptr};  // ns_step_host: history final, step done
   double* stage_f[7] = {};                     // ns_step_host: one staging buffer per state field
@@ -56,6 +57,11 @@ struct ns_handle {
   long long launches = 0;
   bool profiling = false;
   std::vector<std::pair<std::string, cudaEvent_t>> prof_events;
+  // phase trace of ns_step_host (environment variable NS_TRACE set at ns_create):
+  // timed events on the compute and copy streams, printed to stderr per call
+  bool trace = false;
+  std::vector<cudaEvent_t> trace_pool;
+  std::vector<std::string> trace_names;
   // adjoint tier: checkpoints, stored inputs and adjoint fields (owned by ns_adjoint.cu)
   ns::AdjState* adj = nullptr;
 };
