@@ -272,7 +272,10 @@ cudaError_t ensure_xfer(ns_handle* h) {
   const size_t n = (size_t)(h->cfg.nx + 2) * (h->cfg.ny + 2) * (h->cfg.nz + 2);
   if ((e = cudaMalloc(&h->stage2, n * sizeof(double))) != cudaSuccess) return e;
   if ((e = cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking)) != cudaSuccess) return e;
-  if ((e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  int least = 0, greatest = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, least)) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithPriority(&h->prio, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
   for (int b = 0; b < 2; ++b) {
     if ((e = cudaEventCreateWithFlags(&h->ev_full[b], cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming)) != cudaSuccess) return e;
@@ -927,6 +930,7 @@ void free_all(ns_handle* h) {
   if (h->stage2) cudaFree(h->stage2);
   if (h->xfer) cudaStreamDestroy(h->xfer);
   if (h->side) cudaStreamDestroy(h->side);
+  if (h->prio) cudaStreamDestroy(h->prio);
   for (int b = 0; b < 2; ++b) {
     if (h->ev_full[b]) cudaEventDestroy(h->ev_full[b]);
     if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
@@ -1166,14 +1170,24 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     NS_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     h->ev_slab.push_back(e);
   }
+  // The compute runs on the handle's greatest-priority stream (after the
+  // caller's stream): the predictor chain keeps pace with the copies, and the
+  // x and y sweeps on the lowest-priority side stream take the SMs it leaves.
+  trace_mark(h, h->stream, "start");
+  NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_start], h->stream));
+  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[ev_start], 0));
+  NS_CUDA(h, cudaStreamWaitEvent(h->prio, h->ev_slab[ev_start], 0));
+  struct StreamSwap {
+    ns_handle* h;
+    cudaStream_t saved;
+    ~StreamSwap() { h->stream = saved; }
+  } swap{h, h->stream};
+  h->stream = h->prio;
   if (!hist) {
     NS_CUDA(h, cudaMemsetAsync(h->hx, 0, L.fsize * sizeof(double), h->stream));
     NS_CUDA(h, cudaMemsetAsync(h->hy, 0, L.fsize * sizeof(double), h->stream));
     NS_CUDA(h, cudaMemsetAsync(h->hz, 0, L.fsize * sizeof(double), h->stream));
   }
-  trace_mark(h, h->stream, "start");
-  NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_start], h->stream));
-  NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[ev_start], 0));
   auto plane_bytes = [&](int fid) {
     return sizeof(double) * (size_t)ext_of(c, fid, 0) * ext_of(c, fid, 1);
   };
