@@ -66,8 +66,10 @@ __device__ __forceinline__ void finish_line(const LineSys& S, const double* __re
 
 }  // namespace
 
-// x sweep: a warp owns 32 contiguous lines (consecutive y slots at one z
-// slot) and walks them in blocks of 32 unknowns through shared memory.
+// x sweep: a warp owns 32 consecutive lines (line t = j + (ny+2)(k - z0),
+// across plane boundaries, so every warp is full) and walks them in blocks
+// of 32 unknowns through shared memory.  Row l of a block is line t0 + l,
+// whose 32-bit slot offset lane l holds and hands out by shuffle.
 namespace {
 constexpr int XW = 4;           // warps per CTA
 constexpr int XB = 32;          // unknowns per block
@@ -79,25 +81,29 @@ __global__ void __launch_bounds__(32 * XW) adi_x_kernel(AdiArgs a) {
   const int fld = blockIdx.z;
   const LineSys& S = a.sys[fld];
   const Layout L = a.L;
-  const int n1 = L.ny + 2, n2 = L.nz + 2;
+  const int n1 = L.ny + 2;
+  const int nplanes = a.z1 > 0 ? a.z1 - a.z0 : L.nz + 2;
+  const int nlines = n1 * nplanes;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int j0 = (blockIdx.x * XW + warp) * 32;
-  const int k = blockIdx.y + a.z0;
-  if (j0 >= n1) return;
-  const int nl = min(32, n1 - j0);
+  const int t0 = (blockIdx.x * XW + warp) * 32;
+  if (t0 >= nlines) return;
+  const int nl = min(32, nlines - t0);
+  const int t = t0 + min(lane, nl - 1);  // lanes past the end repeat the last line (never stored)
+  const int j = t % n1, k = a.z0 + t / n1;
+  const int my_off = (int)L.at(S.lo, j, k);  // unknown 0 of this lane's line
   double* sb = sh[warp];
   const double* lf = S.l + S.pad;
   const double* di = S.dinv + S.pad;
   const double* cu = S.cu + S.pad;
   const int m = S.hi - S.lo + 1;
   const int nb = (m + XB - 1) / XB;
-  const double* src = a.src[fld] + L.at(S.lo, j0, k);  // unknown 0 of line j0
-  double* dst = a.dst[fld] + L.at(S.lo, j0, k);
-  const long long sy = L.sy;
-  const int plane = (j0 + lane) + n1 * k;
+  const double* src = a.src[fld];
+  double* dst = a.dst[fld];
   const bool act = lane < nl;
+  const bool walls = !S.periodic;
   double face_lo = 0.0, face_hi = 0.0;
-  if (!S.periodic && act) {
+  if (walls && act) {
+    const int plane = j + n1 * k;
     if (a.face_lo[fld]) face_lo = __ldg(a.face_lo[fld] + plane);
     if (a.face_hi[fld]) face_hi = __ldg(a.face_hi[fld] + plane);
   }
@@ -106,51 +112,59 @@ __global__ void __launch_bounds__(32 * XW) adi_x_kernel(AdiArgs a) {
   for (int b = 0; b < nb; ++b) {
     const int e0 = b * XB;
     const int ne = min(XB, m - e0);
-    if (lane < ne)
-      for (int l = 0; l < nl; ++l) sb[lane * XS + l] = __ldg(src + l * sy + e0 + lane);
+#pragma unroll 8
+    for (int l = 0; l < XB; ++l) {
+      const int off = __shfl_sync(0xffffffffu, my_off, l);
+      if (l < nl && lane < ne) sb[lane * XS + l] = __ldg(src + off + e0 + lane);
+    }
     __syncwarp();
+    if (walls) {  // the BC rows take the sweep's face values
+      if (e0 == 0) sb[lane] = face_lo;
+      if (m - 1 - e0 < XB) sb[(m - 1 - e0) * XS + lane] = face_hi;
+    }
     if (act) {
       for (int q = 0; q < ne; ++q) {
-        const int e = e0 + q;
-        double r = sb[q * XS + lane];
-        if (!S.periodic) {
-          if (e == 0) r = face_lo;
-          if (e == m - 1) r = face_hi;
-        }
-        yp = fma(-__ldg(lf + e), yp, r);
+        yp = fma(-__ldg(lf + e0 + q), yp, sb[q * XS + lane]);
         sb[q * XS + lane] = yp;
       }
     }
     __syncwarp();
-    if (lane < ne)
-      for (int l = 0; l < nl; ++l) dst[l * sy + e0 + lane] = sb[lane * XS + l];
+#pragma unroll 8
+    for (int l = 0; l < XB; ++l) {
+      const int off = __shfl_sync(0xffffffffu, my_off, l);
+      if (l < nl && lane < ne) dst[off + e0 + lane] = sb[lane * XS + l];
+    }
     __syncwarp();
   }
-  // back substitution, blocks in reverse
+  // back substitution, blocks in reverse (cu[m-1] = 0 starts the walk)
   double xn = 0.0, x_last = 0.0;
   for (int b = nb - 1; b >= 0; --b) {
     const int e0 = b * XB;
     const int ne = min(XB, m - e0);
-    if (lane < ne)
-      for (int l = 0; l < nl; ++l) sb[lane * XS + l] = dst[l * sy + e0 + lane];
+#pragma unroll 8
+    for (int l = 0; l < XB; ++l) {
+      const int off = __shfl_sync(0xffffffffu, my_off, l);
+      if (l < nl && lane < ne) sb[lane * XS + l] = dst[off + e0 + lane];
+    }
     __syncwarp();
     if (act) {
       for (int q = ne - 1; q >= 0; --q) {
-        const int e = e0 + q;
-        xn = (e == m - 1) ? sb[q * XS + lane] * __ldg(di + e)
-                          : fma(-__ldg(cu + e), xn, sb[q * XS + lane] * __ldg(di + e));
-        if (e == m - 1) x_last = xn;
+        xn = fma(-__ldg(cu + e0 + q), xn, sb[q * XS + lane] * __ldg(di + e0 + q));
         sb[q * XS + lane] = xn;
       }
+      if (b == nb - 1) x_last = sb[(ne - 1) * XS + lane];
     }
     __syncwarp();
-    if (lane < ne)
-      for (int l = 0; l < nl; ++l) dst[l * sy + e0 + lane] = sb[lane * XS + l];
+#pragma unroll 8
+    for (int l = 0; l < XB; ++l) {
+      const int off = __shfl_sync(0xffffffffu, my_off, l);
+      if (l < nl && lane < ne) dst[off + e0 + lane] = sb[lane * XS + l];
+    }
     __syncwarp();
   }
   if (act) {
-    const long long base = L.at(0, j0 + lane, k);
-    finish_line(S, a.src[fld] + base, a.dst[fld] + base, 1, L.nx, xn, x_last);
+    const long long base = L.at(0, j, k);
+    finish_line(S, src + base, dst + base, 1, L.nx, xn, x_last);
   }
 }
 
@@ -262,9 +276,10 @@ cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st) {
     else adi_line_kernel<2, 8><<<grid, 128, 0, st>>>(a);
     return cudaGetLastError();
   }
-  const int n1 = a.L.ny + 2, n2 = a.z1 > 0 ? a.z1 - a.z0 : a.L.nz + 2;
+  const int n2 = a.z1 > 0 ? a.z1 - a.z0 : a.L.nz + 2;
   if (n2 <= 0) return cudaSuccess;
-  dim3 grid((n1 + 32 * XW - 1) / (32 * XW), n2, 3);
+  const long long lines = (long long)(a.L.ny + 2) * n2;
+  dim3 grid((unsigned)((lines + 32 * XW - 1) / (32 * XW)), 1, 3);
   adi_x_kernel<<<grid, 32 * XW, 0, st>>>(a);
   return cudaGetLastError();
 }
