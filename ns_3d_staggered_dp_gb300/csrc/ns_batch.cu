@@ -330,6 +330,7 @@ struct ns_batch {
   double* arena = nullptr;       // fields of all subdomains
   size_t arena_n = 0;
   double* tables = nullptr;      // dense matrices and eigenvalues per size class
+  double2* tri_tab = nullptr;    // z-solve multipliers of every subdomain (one per spectrum entry)
   double* snaps = nullptr;       // n_slots x (all faces)
   double* snap_mean = nullptr;   // n_slots x n
   long long slot_stride = 0;
@@ -556,6 +557,7 @@ int ns_batch_destroy(ns_batch* b) {
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   if (b->arena) cudaFree(b->arena);
   if (b->tables) cudaFree(b->tables);
+  if (b->tri_tab) cudaFree(b->tri_tab);
   if (b->snaps) cudaFree(b->snaps);
   if (b->snap_mean) cudaFree(b->snap_mean);
   if (b->dev_args) cudaFree(b->dev_args);
@@ -690,6 +692,17 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
       cudaSuccess)
     return bail(NS_ERR_CUDA);
 
+  // z-solve multiplier tables, laid out like each subdomain's spectrum
+  std::vector<size_t> tri_off(n);
+  {
+    size_t t = 0;
+    for (int i = 0; i < n; ++i) {
+      tri_off[i] = t;
+      t += align32((size_t)(subs[i].nx / 2) * subs[i].ny * subs[i].nz);
+    }
+    if (cudaMalloc(&b->tri_tab, std::max<size_t>(t, 1) * sizeof(double2)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+  }
+
   // ---- per-subdomain plans and argument tables ----
   const double hs[3] = {c.dx, c.dy, c.dz};
   const int bc3[3] = {c.bc, c.bc, c.bc};
@@ -733,6 +746,8 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     S.has_mean = c.pbc == 3 ? 1 : 0;
     S.mean_val = (double)d.nx * (double)d.ny;
     S.mean_dev = g.mean;
+    if (launch_tri_table(2, S, b->tri_tab + tri_off[i], b->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+    S.tri_m = b->tri_tab + tri_off[i];
     for (int a = 0; a < 3; ++a) {
       const double hh = hs[a];
       if (c.pbc == 2) { S.mod_lo[a] = -2.0 / (hh * hh); S.mod_hi[a] = -2.0 / (hh * hh); }

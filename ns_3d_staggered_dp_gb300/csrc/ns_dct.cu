@@ -322,14 +322,21 @@ __device__ __forceinline__ void tri_solve_body(const SpecPlan& S, double2* __res
   }
   double mr = 0.0, mi = 0.0;
   double2 d = make_double2(0.0, 0.0);
+  const double2* tm = S.tri_m ? S.tri_m + (g - spec) : nullptr;
 #pragma unroll 4
   for (int j = 0; j < N; ++j) {
-    double br = -2.0 + sr, bi = -2.0 + si;
-    if (j == 0) { br += elo; bi += elo; }
-    if (j == N - 1) { br += ehi; bi += ehi; }
-    mr = 1.0 / (br - mr);
-    if (PACKED) mi = 1.0 / (bi - mi);
-    else mi = mr;
+    if (tm) {
+      const double2 mm = __ldg(tm + (long long)j * st);
+      mr = mm.x;
+      mi = mm.y;
+    } else {
+      double br = -2.0 + sr, bi = -2.0 + si;
+      if (j == 0) { br += elo; bi += elo; }
+      if (j == N - 1) { br += ehi; bi += ehi; }
+      mr = 1.0 / (br - mr);
+      if (PACKED) mi = 1.0 / (bi - mi);
+      else mi = mr;
+    }
     const double2 r = g[(long long)j * st];
     d.x = fma(r.x, rs, -d.x) * mr;
     d.y = fma(r.y, rs, -d.y) * mi;
@@ -361,10 +368,93 @@ __global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __re
   extern __shared__ __align__(16) double2 ls_yz[];
   dense_yz_body<AXIS, FWD>(S, spec, ls_yz, blockIdx.x, blockIdx.y);
 }
+// The forward multipliers of tri_solve_body's lines, by its own recurrence
+// (same operations in the same order, so the same bits), into tab at the
+// spectrum index of each entry.  The singular line keeps its own path.
+template <int AXIS, bool PACKED>
+__global__ void __launch_bounds__(TRI_T) tri_table_kernel(SpecPlan S, double2* __restrict__ tab) {
+  const int l = threadIdx.x;
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int N = AXIS == 1 ? S.ny : S.nz;
+  const int n_other = AXIS == 1 ? S.nz : S.ny;
+  const int nreg = PACKED ? S.nxs : S.nxs - 1;
+  const int nblk = (nreg + TRI_T - 1) / TRI_T;
+  int col, o;
+  bool valid;
+  if (bx < nblk) {
+    col = bx * TRI_T + l;
+    o = by;
+    valid = col < nreg;
+  } else {
+    if (by * TRI_T >= n_other) return;
+    col = S.nxs - 1;
+    o = by * TRI_T + l;
+    valid = o < n_other;
+  }
+  if (!valid) return;
+  const long long st = AXIS == 1 ? (long long)S.nxs : (long long)S.nxs * S.ny;
+  double2* g = tab + (AXIS == 1 ? col + (long long)S.nxs * S.ny * o : col + (long long)S.nxs * o);
+  const double lo = __ldg(S.eig_o + o);
+  const double sr = (__ldg(S.eig_x + (PACKED ? 2 * col : col)) + lo) * S.tri_h2;
+  const double si = PACKED ? (__ldg(S.eig_x + 2 * col + 1) + lo) * S.tri_h2 : sr;
+  const double elo = S.tri_elo, ehi = S.tri_ehi;
+  double mr = 0.0, mi = 0.0;
+  for (int j = 0; j < N; ++j) {
+    double br = -2.0 + sr, bi = -2.0 + si;
+    if (j == 0) { br += elo; bi += elo; }
+    if (j == N - 1) { br += ehi; bi += ehi; }
+    mr = 1.0 / (br - mr);
+    if (PACKED) mi = 1.0 / (bi - mi);
+    else mi = mr;
+    g[(long long)j * st] = make_double2(mr, mi);
+  }
+}
+
 template <int AXIS, bool PACKED>
 __global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* __restrict__ spec) {
   extern __shared__ __align__(16) double cm_tri[];
   tri_solve_body<AXIS, PACKED>(S, spec, cm_tri, blockIdx.x, blockIdx.y);
+}
+
+// The z solve of a packed-x box with its multiplier table (S.tri_m), one
+// thread per line over the flattened (x column, y mode) index t = col + nxs*o:
+// full warps whatever nxs is, and no shared memory but the singular line's
+// scratch (cm, thread 0 of block 0).  Same operations as tri_solve_body.
+__device__ __forceinline__ void tri_lines_body(const SpecPlan& S, double2* __restrict__ spec, double* cm, int bx) {
+  const int N = S.nz;
+  const int t = bx * blockDim.x + threadIdx.x;
+  if (t >= S.nxs * S.ny) return;
+  const long long st = (long long)S.nxs * S.ny;
+  double2* g = spec + t;
+  const double rs = S.tri_rs;
+  if (S.has_mean && t == 0) {  // the singular line (col 0, o 0): its own path
+    const double lo = __ldg(S.eig_o);
+    const double sr = (__ldg(S.eig_x) + lo) * S.tri_h2;
+    const double si = (__ldg(S.eig_x + 1) + lo) * S.tri_h2;
+    double* x = reinterpret_cast<double*>(g);
+    tri_real(x, 2 * st, N, sr, S.tri_elo, S.tri_ehi, rs, cm, true, S.mean_dev ? S.mean_val * *S.mean_dev : S.mean_val);
+    tri_real(x + 1, 2 * st, N, si, S.tri_elo, S.tri_ehi, rs, cm + (long long)N * TRI_T, false, 0.0);
+    return;
+  }
+  const double2* __restrict__ tm = S.tri_m + t;
+  double2 d = make_double2(0.0, 0.0);
+#pragma unroll 4
+  for (int j = 0; j < N; ++j) {
+    const double2 mm = __ldg(tm + (long long)j * st);
+    const double2 r = g[(long long)j * st];
+    d.x = fma(r.x, rs, -d.x) * mm.x;
+    d.y = fma(r.y, rs, -d.y) * mm.y;
+    g[(long long)j * st] = d;
+  }
+  double2 p = d;
+#pragma unroll 4
+  for (int j = N - 2; j >= 0; --j) {
+    const double2 mm = __ldg(tm + (long long)j * st);
+    const double2 x = g[(long long)j * st];
+    p.x = fma(-mm.x, p.x, x.x);
+    p.y = fma(-mm.y, p.y, x.y);
+    g[(long long)j * st] = p;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -385,7 +475,7 @@ __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __
     if (PASS == 1) dense_x_inv_body(a.S, a.spec, a.dp, a.L, sm_b, w.bx);
     if (PASS == 2) dense_yz_body<1, true>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);
     if (PASS == 3) dense_yz_body<1, false>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);
-    if (PASS == 4 && threadIdx.x < TRI_T) tri_solve_body<2, true>(a.S, a.spec, sm_b, w.bx, w.by);
+    if (PASS == 4) tri_lines_body(a.S, a.spec, sm_b, w.bx);
     __syncthreads();
   }
 }
@@ -395,7 +485,7 @@ void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
   gy = 1;
   if (pass == 0 || pass == 1) gx = (S.ny * S.nz + 3) / 4;
   else if (pass == 2 || pass == 3) { gx = (S.nxs + 15) / 16; gy = S.nz; }
-  else { gx = (S.nxs + TRI_T - 1) / TRI_T; gy = S.ny; }
+  else gx = (S.nxs * S.ny + 127) / 128;  // tri_lines_body: 128 lines per item
 }
 
 size_t spec_pass_smem(int pass, const SpecPlan& S) {
@@ -418,11 +508,11 @@ cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchIte
     int per_sm = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, pass == 4 ? TRI_T : 128, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem);
     grid = (per_sm > 0 ? per_sm : 1) * nsm;
   }
   if (grid > n_items) grid = n_items;
-  kern<<<grid, pass == 4 ? TRI_T : 128, smem, st>>>(tab, items, n_items);
+  kern<<<grid, 128, smem, st>>>(tab, items, n_items);
   return cudaGetLastError();
 }
 
@@ -459,6 +549,22 @@ cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec
   else if (axis == 1) dense_yz_kernel<1, false><<<grid, 128, sm, st>>>(S, spec);
   else if (fwd) dense_yz_kernel<2, true><<<grid, 128, sm, st>>>(S, spec);
   else dense_yz_kernel<2, false><<<grid, 128, sm, st>>>(S, spec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tri_table(int axis, const SpecPlan& S, double2* tab, cudaStream_t st) {
+  const int n_other = axis == 1 ? S.nz : S.ny;
+  const bool packed = S.kind[0] != 0;
+  const int nreg = packed ? S.nxs : S.nxs - 1;
+  const int nblk = (nreg + TRI_T - 1) / TRI_T;
+  dim3 grid(nblk + (packed ? 0 : 1), n_other);
+  if (axis == 1) {
+    if (packed) tri_table_kernel<1, true><<<grid, TRI_T, 0, st>>>(S, tab);
+    else tri_table_kernel<1, false><<<grid, TRI_T, 0, st>>>(S, tab);
+  } else {
+    if (packed) tri_table_kernel<2, true><<<grid, TRI_T, 0, st>>>(S, tab);
+    else tri_table_kernel<2, false><<<grid, TRI_T, 0, st>>>(S, tab);
+  }
   return cudaGetLastError();
 }
 

@@ -200,6 +200,8 @@ struct FftPlan {
   double tri_h2;          // h_s^2
   double tri_rs;          // h_s^2 * scale of the unnormalised FFT passes
   double tri_elo, tri_ehi;  // end-row diagonal changes: pbc 2 -1, pbc 3 +1, pbc 4 0
+  const double2* tri_m;   // non-null: the forward multipliers (re, im) of every line, laid out like the
+                          // spectrum (launch_tri_table), read instead of computed
   double mod_lo[3], mod_hi[3];        // pr_bc_staggered_modify_rhs coefficients per axis
   const double* face_lo[3];           // pressure face planes per axis (internal slot order)
   const double* face_hi[3];
@@ -260,6 +262,10 @@ cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double
 cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st);
 // Tridiagonal solve of every spectrum line along axis 1 (y) or 2 (z) (ns_dct.cu).
 cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st);
+// The multipliers of those lines (they depend on the mode and the matrix, not
+// on the data), computed by the solve's own recurrence into tab (one double2
+// per spectrum entry); then set S.tri_m = tab.
+cudaError_t launch_tri_table(int axis, const SpecPlan& S, double2* tab, cudaStream_t st);
 // Batched spectral passes of all-wall boxes (x dense packed, y dense, z line solve).
 struct BatchSpecArgs {
   SpecPlan S;
