@@ -466,11 +466,11 @@ template <int PASS>
 __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __restrict__ tab,
                                                          const BatchItem* __restrict__ items, int n_items) {
   extern __shared__ __align__(16) double sm_b[];
-  __shared__ BatchSpecArgs a;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const BatchItem w = items[it];
-    if (threadIdx.x == 0) a = tab[w.sub];
-    __syncthreads();
+    // the subdomain's arguments from the read-only table (a copy in shared
+    // memory would be reloaded after every barrier of the passes)
+    const BatchSpecArgs& a = tab[w.sub];
     if (PASS == 0) dense_x_fwd_body(a.S, a.d, a.spec, sm_b, w.bx);
     if (PASS == 1) dense_x_inv_body(a.S, a.spec, a.dp, a.L, sm_b, w.bx);
     if (PASS == 2) dense_yz_body<1, true>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);

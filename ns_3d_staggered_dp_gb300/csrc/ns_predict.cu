@@ -262,14 +262,15 @@ __global__ void __launch_bounds__(TX*(TY + 1)) predict_kernel(PredictArgs a) {
 
 // Batched: persistent CTAs walk the work items (subdomain, tile) of a batch.
 template <int SCHEME, bool FIRST, bool DPF>
-__global__ void __launch_bounds__(TX*(TY + 1)) predict_batch_kernel(const PredictArgs* __restrict__ tab,
-                                                                    const BatchItem* __restrict__ items, int n_items) {
+__global__ void __launch_bounds__(TX*(TY + 1), 2) predict_batch_kernel(const PredictArgs* __restrict__ tab,
+                                                                       const BatchItem* __restrict__ items,
+                                                                       int n_items) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ PredictArgs a;
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const BatchItem w = items[it];
-    if (threadIdx.x == 0 && threadIdx.y == 0) a = tab[w.sub];
-    __syncthreads();
+    // the subdomain's arguments in registers: a reference into shared memory
+    // would be reloaded after every barrier of the plane loop
+    const PredictArgs a = tab[w.sub];
     predict_body<SCHEME, FIRST, DPF, 0>(a, *reinterpret_cast<PredSmem*>(smem_raw), w.bx, w.by, w.bz);
     __syncthreads();
   }
