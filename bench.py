@@ -77,7 +77,7 @@ FP64_LANES_PER_CLK_SM = 2  # DFMA issue rate of this part (ncu ..._op_dfma_pred_
 # DRAM bytes per launch at 256^3 (dram__bytes_read.sum + dram__bytes_write.sum)
 # from one ncu capture of each kernel of this build's step.
 NCU_TRAFFIC_256 = {
-    "predict": 1659.0e6, "adi_x": 1474.7e6, "adi_y": 1486.3e6, "adi_z": 1480.0e6,
+    "predict": 1659.0e6, "adi_x": 1574.2e6, "adi_y": 1486.3e6, "adi_z": 1480.0e6,
     "fft_x_fwd": 533.7e6, "fft_y_fwd": 213.0e6, "fft_z_solve": 293.6e6, "fft_y_inv": 213.0e6,
     "fft_x_inv": 219.9e6, "correct": 1112.1e6,
 }
