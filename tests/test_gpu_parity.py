@@ -51,7 +51,11 @@ def test_cal_conv_diff(g):
         assert rel_l2(a, b) < ROUTINE_TOL
 
 
-@pytest.mark.parametrize("g", GRIDS + [(16, 16, 16, 1.0, 1.0, 1.0), (64, 32, 16, 1.0, 1.0, 1.0)])
+# the largest FFT axis the library accepts (512) on each axis in turn
+MAX_FFT_GRIDS = [(512, 16, 16, 2.0, 1.0, 1.0), (16, 512, 16, 1.0, 2.0, 1.0), (16, 16, 512, 1.0, 1.0, 2.0)]
+
+
+@pytest.mark.parametrize("g", GRIDS + [(16, 16, 16, 1.0, 1.0, 1.0), (64, 32, 16, 1.0, 1.0, 1.0)] + MAX_FFT_GRIDS)
 def test_fft_poisson(g):
     nx, ny, nz, fx, fy, fz = g
     cfg = O.Config(nx, ny, nz, lx=2 * np.pi * fx, ly=2 * np.pi * fy, lz=2 * np.pi * fz)
@@ -113,6 +117,17 @@ def _run_compare(cfg, st, nsteps, **kw):
         err = rel_l2(got[k], r)
         assert err < STEP_TOL, (k, err)
     return got, ref
+
+
+@pytest.mark.parametrize("g", MAX_FFT_GRIDS)
+def test_step_max_fft_axis(g):
+    """Two AB2-CN steps with a 512-cell periodic axis (the largest FFT, the
+    longest ADI lines) against the oracle."""
+    nx, ny, nz, fx, fy, fz = g
+    cfg = O.Config(nx, ny, nz, lx=2 * np.pi * fx, ly=2 * np.pi * fy, lz=2 * np.pi * fz, nu=0.02, dt=0.002,
+                   scheme=O.AB2_CN)
+    st = random_state(cfg, 17, history=True)
+    _run_compare(cfg, st, 2)
 
 
 @pytest.mark.parametrize("scheme", [O.EULER, O.AB2, O.AB2_CN])

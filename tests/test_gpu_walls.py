@@ -56,6 +56,11 @@ POISSON_CASES = [
     ((16, 32, 256), (1, 1, 2)),
     ((32, 128, 200), (1, 4, 3)),
     ((64, 64, 64), (3, 3, 3)),
+    # the size limits: the wall axis solved by lines (512), a dense y in front of it (128),
+    # a dense x (1024, with its line axis limited to 256)
+    ((16, 16, 512), (1, 1, 3)),
+    ((16, 128, 512), (1, 2, 4)),
+    ((1024, 16, 16), (3, 3, 3)),
 ]
 
 
