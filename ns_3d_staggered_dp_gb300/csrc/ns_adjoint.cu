@@ -230,16 +230,15 @@ __global__ void __launch_bounds__(32 * PH, 3) adj_predict_kernel(AdjArgs a) {
 // products).  At 128^3 this gives 7 chunks of 19 planes (448 CTAs on 456
 // slots) instead of 8 chunks (512 CTAs, 1.12 waves).
 static int adj_chunk(int cols, int nz, int slots) {
-  int best = nz, bc = 1;
+  int best = nz;
   double best_t = 1e300;
   for (int c = 1; c <= nz; ++c) {
     const int kc = (nz + c - 1) / c;
     const int cc = (nz + kc - 1) / kc;  // chunks actually launched
     const double waves = std::ceil((double)cols * cc / slots);
     const double t = waves * (kc + 2);
-    if (t < best_t - 1e-9) { best_t = t; best = kc; bc = cc; }
+    if (t < best_t - 1e-9) { best_t = t; best = kc; }
   }
-  (void)bc;
   return best;
 }
 

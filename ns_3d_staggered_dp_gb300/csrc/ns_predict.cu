@@ -148,7 +148,7 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
 
   const int i = i0 + lane;
   const int j = j0 - 1 + wy;
-  const int nx = L.nx, ny = L.ny, nz = L.nz;
+  const int nx = L.nx, ny = L.ny;
   const bool in_xy = (wy >= 1) && (i <= nx) && (j <= ny);
   const bool act_u = in_xy && (i >= a.ulo);
   const bool act_v = in_xy && (j >= a.vlo);
