@@ -322,21 +322,14 @@ __device__ __forceinline__ void tri_solve_body(const SpecPlan& S, double2* __res
   }
   double mr = 0.0, mi = 0.0;
   double2 d = make_double2(0.0, 0.0);
-  const double2* tm = S.tri_m ? S.tri_m + (g - spec) : nullptr;
 #pragma unroll 4
   for (int j = 0; j < N; ++j) {
-    if (tm) {
-      const double2 mm = __ldg(tm + (long long)j * st);
-      mr = mm.x;
-      mi = mm.y;
-    } else {
-      double br = -2.0 + sr, bi = -2.0 + si;
-      if (j == 0) { br += elo; bi += elo; }
-      if (j == N - 1) { br += ehi; bi += ehi; }
-      mr = 1.0 / (br - mr);
-      if (PACKED) mi = 1.0 / (bi - mi);
-      else mi = mr;
-    }
+    double br = -2.0 + sr, bi = -2.0 + si;
+    if (j == 0) { br += elo; bi += elo; }
+    if (j == N - 1) { br += ehi; bi += ehi; }
+    mr = 1.0 / (br - mr);
+    if (PACKED) mi = 1.0 / (bi - mi);
+    else mi = mr;
     const double2 r = g[(long long)j * st];
     d.x = fma(r.x, rs, -d.x) * mr;
     d.y = fma(r.y, rs, -d.y) * mi;

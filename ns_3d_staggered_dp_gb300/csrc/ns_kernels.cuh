@@ -200,8 +200,8 @@ struct FftPlan {
   double tri_h2;          // h_s^2
   double tri_rs;          // h_s^2 * scale of the unnormalised FFT passes
   double tri_elo, tri_ehi;  // end-row diagonal changes: pbc 2 -1, pbc 3 +1, pbc 4 0
-  const double2* tri_m;   // non-null: the forward multipliers (re, im) of every line, laid out like the
-                          // spectrum (launch_tri_table), read instead of computed
+  const double2* tri_m;   // the forward multipliers (re, im) of every line, laid out like the spectrum
+                          // (launch_tri_table); read by the batched z solve (tri_lines_body)
   double mod_lo[3], mod_hi[3];        // pr_bc_staggered_modify_rhs coefficients per axis
   const double* face_lo[3];           // pressure face planes per axis (internal slot order)
   const double* face_hi[3];

@@ -36,7 +36,6 @@ struct ns_handle {
   double* stage_f[7] = {};                     // ns_step_host: one staging buffer per state field
   std::vector<cudaEvent_t> ev_slab;            // ns_step_host: one event per z-slab
   double* inv_lam = nullptr;
-  double2* tri_tab = nullptr;  // multipliers of the wall-axis line solve (one per spectrum entry)
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
   ns::FftPlan plan{};
   // ADI factors
