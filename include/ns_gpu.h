@@ -39,7 +39,8 @@ enum {
   NS_ERR_SHAPE = 1,          /* unsupported / inconsistent grid size            */
   NS_ERR_CUDA = 2,           /* a CUDA runtime call failed                      */
   NS_ERR_NONFINITE = 3,      /* NaN/Inf found by a checked call                 */
-  NS_ERR_TIMEOUT = 4,        /* a bounded device wait ran out                   */
+  NS_ERR_TIMEOUT = 4,        /* a bounded device wait ran out (no kernel of this
+                                build waits on a flag, so none returns it)       */
   NS_ERR_UNSUPPORTED_BC = 5, /* bc/pbc/scheme combination the step cannot run   */
   NS_ERR_ARG = 6,            /* NULL or out-of-range argument                   */
   NS_ERR_NOMEM = 7           /* device allocation failed                        */

@@ -53,30 +53,33 @@ __device__ __forceinline__ double rhs_cell(const DivArgs& d, const SpecPlan& S, 
 // One warp per line (j, k); lane q computes the modes 2q' and 2q'+1.
 __device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArgs& d, double2* __restrict__ spec,
                                                  double* xs, int bx) {
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int line = bx * 4 + warp;
+  // a group of G lanes per line, 128/G lines per CTA (several short lines share a warp)
+  const int G = dense_x_group(S.nx);
+  const int grp = threadIdx.x / G, gl = threadIdx.x % G;
+  const int line = bx * (128 / G) + grp;
   const int nx = S.nx, ny = S.ny, nz = S.nz;
   const bool valid = line < ny * nz;
   const int j = valid ? 1 + line % ny : 1, k = valid ? 1 + line / ny : 1;
-  double* r = xs + warp * nx;
+  double* r = xs + grp * nx;
   const FOne c{d.one, d.mzero};
   if (valid)
-    for (int i = lane; i < nx; i += 32) r[i] = rhs_cell(d, S, c, i + 1, j, k);
+    for (int i = gl; i < nx; i += G) r[i] = rhs_cell(d, S, c, i + 1, j, k);
   __syncwarp();
-  if (!valid) return;
   const double* __restrict__ FT = S.fwd[0];  // F^T: FT[n * N + kk] = F[kk][n]
   double2* out = spec + (long long)S.nxs * ((j - 1) + (long long)ny * (k - 1));
   if (S.sym[0] & 1) {
     // F[k][N-1-n] = (-1)^k F[k][n]: fold the line (s[n] = r[n] + r[N-1-n] at n,
     // d[n] = r[n] - r[N-1-n] at N-1-n); mode 2q sums F s, mode 2q+1 sums F d
     const int H = nx / 2;
-    for (int n = lane; n < H; n += 32) {
-      const double a0 = r[n], b0 = r[nx - 1 - n];
-      r[n] = a0 + b0;
-      r[nx - 1 - n] = a0 - b0;
-    }
+    if (valid)
+      for (int n = gl; n < H; n += G) {
+        const double a0 = r[n], b0 = r[nx - 1 - n];
+        r[n] = a0 + b0;
+        r[nx - 1 - n] = a0 - b0;
+      }
     __syncwarp();
-    for (int q = lane; q < H; q += 32) {
+    if (!valid) return;
+    for (int q = gl; q < H; q += G) {
       double a = 0.0, b = 0.0;
       for (int n = 0; n < H; ++n) {
         const double2 f = *reinterpret_cast<const double2*>(FT + (long long)n * nx + 2 * q);
@@ -87,7 +90,8 @@ __device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArg
     }
     return;
   }
-  for (int q = lane; q < nx / 2; q += 32) {
+  if (!valid) return;
+  for (int q = gl; q < nx / 2; q += G) {
     double a = 0.0, b = 0.0;
     for (int n = 0; n < nx; ++n) {
       const double2 f = *reinterpret_cast<const double2*>(FT + (long long)n * nx + 2 * q);
@@ -101,15 +105,16 @@ __device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArg
 // x inverse for a non-periodic x axis: packed modes -> G_x -> dp slots 1..nx.
 __device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double2* __restrict__ spec, double* dp,
                                                  const Layout& L, double* xs, int bx) {
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int line = bx * 4 + warp;
+  const int G = dense_x_group(S.nx);
+  const int grp = threadIdx.x / G, gl = threadIdx.x % G;
+  const int line = bx * (128 / G) + grp;
   const int nx = S.nx, ny = S.ny, nz = S.nz;
   const bool valid = line < ny * nz;
   const int j = valid ? 1 + line % ny : 1, k = valid ? 1 + line / ny : 1;
-  double* X = xs + warp * nx;
+  double* X = xs + grp * nx;
   const double2* in = spec + (long long)S.nxs * ((j - 1) + (long long)ny * (k - 1));
   if (valid)
-    for (int q = lane; q < nx / 2; q += 32) {
+    for (int q = gl; q < nx / 2; q += G) {
       const double2 v = in[q];
       X[2 * q] = v.x;
       X[2 * q + 1] = v.y;
@@ -120,7 +125,7 @@ __device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double
   double* o = dp + L.at(1, j, k);
   if (S.sym[0] & 2) {
     // G[N-1-n][k] = (-1)^k G[n][k]: out[n] = E + O, out[N-1-n] = E - O
-    for (int n = lane; n < nx / 2; n += 32) {
+    for (int n = gl; n < nx / 2; n += G) {
       double e = 0.0, od = 0.0;
       for (int kk = 0; kk + 1 < nx; kk += 2) {
         e = fma(__ldg(GT + (long long)kk * nx + n), X[kk], e);
@@ -131,23 +136,27 @@ __device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double
     }
     return;
   }
-  for (int n = lane; n < nx; n += 32) {
+  for (int n = gl; n < nx; n += G) {
     double a = 0.0;
     for (int kk = 0; kk < nx; ++kk) a = fma(__ldg(GT + (long long)kk * nx + n), X[kk], a);
     o[n] = a;
   }
 }
 
-// Dense transform of complex lines along y (AXIS 1) or z (AXIS 2), lanes over
-// consecutive spectrum columns (coalesced).
+// Dense transform of complex lines along y (AXIS 1) or z (AXIS 2).  Lines are
+// numbered t = col + nxs * o (o: z for y-lines, y for z-lines) and a CTA takes
+// 16 consecutive ones, so narrow spectra fill it too; neighbouring lanes read
+// neighbouring columns (coalesced).
 template <int AXIS, bool FWD>
-__device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __restrict__ spec, double2* ls, int bx, int by) {
-  constexpr int LPC = 16, T = 8;  // 16 lines (columns) x 8 threads per line
+__device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __restrict__ spec, double2* ls, int bx) {
+  constexpr int LPC = 16, T = 8;  // 16 lines x 8 threads per line
   const int l = threadIdx.x % LPC, t = threadIdx.x / LPC;
   const int N = (AXIS == 1) ? S.ny : S.nz;
-  const int col = bx * LPC + l;
-  const bool valid = col < S.nxs;
-  const int o = by;  // the other index (z for y-lines, y for z-lines)
+  const int n_other = (AXIS == 1) ? S.nz : S.ny;
+  const int tl = bx * LPC + l;
+  const bool valid = tl < S.nxs * n_other;
+  const int col = valid ? tl % S.nxs : 0;
+  const int o = valid ? tl / S.nxs : 0;
   const long long st = (AXIS == 1) ? (long long)S.nxs : (long long)S.nxs * S.ny;
   const long long base = (AXIS == 1) ? col + (long long)S.nxs * S.ny * o : col + (long long)S.nxs * o;
   double2* line = ls + l;  // element n at line[n * LPC]
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(128) dense_x_inv_kernel(SpecPlan S, const doub
 template <int AXIS, bool FWD>
 __global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __restrict__ spec) {
   extern __shared__ __align__(16) double2 ls_yz[];
-  dense_yz_body<AXIS, FWD>(S, spec, ls_yz, blockIdx.x, blockIdx.y);
+  dense_yz_body<AXIS, FWD>(S, spec, ls_yz, blockIdx.x);
 }
 // The forward multipliers of tri_solve_body's lines, by its own recurrence
 // (same operations in the same order, so the same bits), into tab at the
@@ -466,8 +475,8 @@ __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __
     const BatchSpecArgs& a = tab[w.sub];
     if (PASS == 0) dense_x_fwd_body(a.S, a.d, a.spec, sm_b, w.bx);
     if (PASS == 1) dense_x_inv_body(a.S, a.spec, a.dp, a.L, sm_b, w.bx);
-    if (PASS == 2) dense_yz_body<1, true>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);
-    if (PASS == 3) dense_yz_body<1, false>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx, w.by);
+    if (PASS == 2) dense_yz_body<1, true>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx);
+    if (PASS == 3) dense_yz_body<1, false>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx);
     if (PASS == 4) tri_lines_body(a.S, a.spec, sm_b, w.bx);
     __syncthreads();
   }
@@ -476,13 +485,16 @@ __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __
 // Work-item grid of one pass for one subdomain.
 void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
   gy = 1;
-  if (pass == 0 || pass == 1) gx = (S.ny * S.nz + 3) / 4;
-  else if (pass == 2 || pass == 3) { gx = (S.nxs + 15) / 16; gy = S.nz; }
+  if (pass == 0 || pass == 1) {
+    const int per = 128 / dense_x_group(S.nx);
+    gx = (S.ny * S.nz + per - 1) / per;
+  }
+  else if (pass == 2 || pass == 3) gx = (S.nxs * S.nz + 15) / 16;  // dense_yz_body: 16 lines per item
   else gx = (S.nxs * S.ny + 127) / 128;  // tri_lines_body: 128 lines per item
 }
 
 size_t spec_pass_smem(int pass, const SpecPlan& S) {
-  if (pass == 0 || pass == 1) return (size_t)4 * S.nx * sizeof(double);
+  if (pass == 0 || pass == 1) return (size_t)(128 / dense_x_group(S.nx)) * S.nx * sizeof(double);
   if (pass == 2 || pass == 3) return (size_t)S.ny * 16 * sizeof(double2);
   return (size_t)S.nz * TRI_T * sizeof(double) * 2;
 }
@@ -511,10 +523,10 @@ cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchIte
 
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                            cudaStream_t st) {
-  const int lines = S.ny * S.nz;
-  const size_t sm = (size_t)4 * S.nx * sizeof(double);
-  if (fwd) dense_x_fwd_kernel<<<(lines + 3) / 4, 128, sm, st>>>(S, d, spec);
-  else dense_x_inv_kernel<<<(lines + 3) / 4, 128, sm, st>>>(S, spec, dp, L);
+  const int lines = S.ny * S.nz, per = 128 / dense_x_group(S.nx);
+  const size_t sm = (size_t)per * S.nx * sizeof(double);
+  if (fwd) dense_x_fwd_kernel<<<(lines + per - 1) / per, 128, sm, st>>>(S, d, spec);
+  else dense_x_inv_kernel<<<(lines + per - 1) / per, 128, sm, st>>>(S, spec, dp, L);
   return cudaGetLastError();
 }
 
@@ -537,7 +549,7 @@ cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec
   const int N = axis == 1 ? S.ny : S.nz;
   if (N > 128) return cudaErrorInvalidValue;
   const size_t sm = (size_t)N * 16 * sizeof(double2);
-  dim3 grid((S.nxs + 15) / 16, axis == 1 ? S.nz : S.ny);
+  dim3 grid((S.nxs * (axis == 1 ? S.nz : S.ny) + 15) / 16);
   if (axis == 1 && fwd) dense_yz_kernel<1, true><<<grid, 128, sm, st>>>(S, spec);
   else if (axis == 1) dense_yz_kernel<1, false><<<grid, 128, sm, st>>>(S, spec);
   else if (fwd) dense_yz_kernel<2, true><<<grid, 128, sm, st>>>(S, spec);

@@ -256,6 +256,14 @@ cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec
 // Symmetry bits of a dense transform pair of even size n (sym in FftPlan),
 // checked entry by entry on the host (ns_dct.cu).
 int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double>& G);
+// Lanes per x line of the dense x passes: the next power of two at or above
+// nx/2 (the mode pairs of a line), at most 32; a 128-thread CTA takes 128/G lines.
+__host__ __device__ __forceinline__ int dense_x_group(int nx) {
+  const int h = nx / 2 > 1 ? nx / 2 : 1;
+  int g = 1;
+  while (g < h && g < 32) g <<= 1;
+  return g;
+}
 // Dense passes (ns_dct.cu): x forward/inverse, y/z forward/inverse.
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                            cudaStream_t st);

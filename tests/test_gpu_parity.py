@@ -218,3 +218,23 @@ def test_step_host_in_place(n):
             assert all(got[k].ctypes.data == ptrs[k] for k in arrs)  # really in place
     for k in ref:
         assert np.array_equal(arrs[k], ref[k]), k
+
+
+def test_nonfinite_state_is_reported():
+    """A NaN in the state spreads through the step; ns_get_diag reports it as
+    NS_ERR_NONFINITE (the divergence maximum orders a NaN above every
+    finite value) and the handle stays usable."""
+    from ns_3d_staggered_dp_gb300 import NSError
+    cfg = O.Config(16, 16, 16, nu=0.02, dt=0.01, scheme=O.AB2_CN)
+    st = random_state(cfg, 5)
+    bad = st.u.copy()
+    bad[5, 6, 7] = np.nan
+    with session(cfg) as s:
+        s.set_state(bad, st.v, st.w, st.p)
+        s.step(1)
+        with pytest.raises(NSError) as e:
+            s.diag()
+        assert e.value.status == 3
+        s.set_state(st.u, st.v, st.w, st.p)  # the same handle runs a clean step afterwards
+        s.step(1)
+        assert s.diag()["max_div"] < 1e-10
