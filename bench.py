@@ -667,6 +667,11 @@ def run_ours(args):
         dpf = int(W["config"].get("dp_flag", 0))
         h2d = sum(a.nbytes for k, a in hin.items() if k != "p" or dpf) + sum(a.nbytes for a in hhist)
         d2h = sum(a.nbytes for a in hout.values()) + sum(a.nbytes for a in hout_h)
+        # one untimed call first: it allocates the per-field staging buffers
+        s._check(lib.ns_step_host(s.h, P(hin["u"]), P(hin["v"]), P(hin["w"]), P(hin["p"]),
+                                  P(hhist[0]), P(hhist[1]), P(hhist[2]),
+                                  P(hout["u"]), P(hout["v"]), P(hout["w"]), P(hout["p"]),
+                                  P(hout_h[0]), P(hout_h[1]), P(hout_h[2])))
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()

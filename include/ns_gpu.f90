@@ -22,7 +22,8 @@ module ns_gpu
     integer(c_int) :: dp_flag, gauge
     real(c_double) :: mean_dp
     integer(c_int) :: cn_periodic_closure, use_graph
-    integer(c_int) :: reserved(8)
+    integer(c_int) :: poisson_z
+    integer(c_int) :: reserved(7)
   end type ns_config
 
   type, bind(C) :: ns_diag

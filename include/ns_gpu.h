@@ -70,7 +70,10 @@ typedef struct ns_config {
   int cn_periodic_closure; /* 0: reference closure of the periodic normal-component
                               CN row, A(1,n+1) (NS_functions.f90:1273); 1: A(1,n)   */
   int use_graph;        /* 1: replay each step from a captured CUDA graph          */
-  int reserved[8];
+  int poisson_z;        /* all-periodic boxes, the z stage of the Poisson solve:
+                           0: cyclic tridiagonal line solves (Sherman-Morrison),
+                           1: z FFT, divide by the eigenvalue, z IFFT            */
+  int reserved[7];
 } ns_config;
 
 /* Diagnostics (big_periodic_3D.f90:572-579). */

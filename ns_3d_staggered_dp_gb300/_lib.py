@@ -27,7 +27,8 @@ class NSConfig(C.Structure):
         ("mean_dp", C.c_double),
         ("cn_periodic_closure", C.c_int),
         ("use_graph", C.c_int),
-        ("reserved", C.c_int * 8),
+        ("poisson_z", C.c_int),
+        ("reserved", C.c_int * 7),
     ]
 
 

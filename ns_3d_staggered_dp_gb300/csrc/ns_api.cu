@@ -436,6 +436,7 @@ void face_to_plane(const ns_config& c, const Layout& L, int axis, int field, con
 int validate(const ns_config& c, std::string& msg) {
   if (c.nx < 4 || c.ny < 4 || c.nz < 4) { msg = "grid too small"; return NS_ERR_SHAPE; }
   if (c.scheme < 0 || c.scheme > 2) { msg = "scheme must be 0 (Euler), 1 (AB2) or 2 (AB2-CN)"; return NS_ERR_ARG; }
+  if (c.poisson_z != 0 && c.poisson_z != 1) { msg = "poisson_z must be 0 (cyclic line solves) or 1 (z FFT)"; return NS_ERR_ARG; }
   for (int a = 0; a < 3; ++a) {
     if (c.bc[a] != 1 && c.bc[a] != 2 && c.bc[a] != 4) {
       msg = "velocity bc must be 1, 2 or 4 (3 leaves the ghosts undefined in the reference)";
@@ -836,6 +837,13 @@ int build_plans(ns_handle* h) {
     for (int a = 0; a < 3; ++a)
       if (a != sax && P.kind[a] == 1) dense_other *= n3[a];
     P.mean_val = c.mean_dp * dense_other;  // mean of the singular line
+  } else if (allper && c.poisson_z == 0) {
+    // cyclic z solve: the x and y eigenvalues give each z line's diagonal
+    o_ex = tab.size();
+    tab.insert(tab.end(), e3[0].begin(), e3[0].end());
+    o_eo = tab.size();
+    tab.insert(tab.end(), e3[1].begin(), e3[1].end());
+    P.mean_val = 0.0;
   } else {
     o_il = tab.size();
     tab.resize(tab.size() + nspec);
@@ -856,9 +864,10 @@ int build_plans(ns_handle* h) {
   const double* t0 = h->inv_lam;
   P.nx = nx; P.ny = ny; P.nz = nz; P.nxh = nxh; P.nxs = nxs;
   P.tw_x = h->tw; P.tw_xr = h->tw + o_xr; P.tw_y = h->tw + o_y; P.tw_z = h->tw + o_z;
-  P.inv_lam = sax ? nullptr : t0 + o_il;
-  P.eig_x = sax ? t0 + o_ex : nullptr;
-  P.eig_o = sax ? t0 + o_eo : nullptr;
+  const bool zcyc = !sax && allper && c.poisson_z == 0;
+  P.inv_lam = (sax || zcyc) ? nullptr : t0 + o_il;
+  P.eig_x = (sax || zcyc) ? t0 + o_ex : nullptr;
+  P.eig_o = (sax || zcyc) ? t0 + o_eo : nullptr;
   for (int a = 0; a < 3; ++a) {
     P.fwd[a] = P.kind[a] == 1 ? t0 + o_f[a] : nullptr;
     P.inv[a] = P.kind[a] == 1 ? t0 + o_g[a] : nullptr;
@@ -873,6 +882,14 @@ int build_plans(ns_handle* h) {
     else if (c.pbc[a] == 4) { P.mod_lo[a] = -1.0 / (hh * hh); P.mod_hi[a] = -1.0 / (hh * hh); }
     P.face_lo[a] = h->faces[0].ax[a].f[3][0];
     P.face_hi[a] = h->faces[0].ax[a].f[3][1];
+  }
+  if (zcyc) {
+    P.zcyc = 1;
+    P.cyc_h2 = h->dz * h->dz;
+    P.cyc_rs = h->dz * h->dz * scale * nz;
+    NS_CUDA(h, cudaMalloc(&h->cyc_buf, cyc_table_doubles(P) * sizeof(double)));
+    NS_CUDA(h, launch_cyc_table(P, h->cyc_buf, h->stream));
+    NS_CUDA(h, cudaStreamSynchronize(h->stream));
   }
   // The wall-axis line solve computes its multipliers: with a warp per 32
   // lines and 32 warps per SM the division chain is hidden, and a table
@@ -931,6 +948,7 @@ void free_all(ns_handle* h) {
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (h->spec) cudaFree(h->spec);
+  if (h->cyc_buf) cudaFree(h->cyc_buf);
   if (h->stage) cudaFree(h->stage);
   if (h->stage2) cudaFree(h->stage2);
   if (h->xfer) cudaStreamDestroy(h->xfer);

@@ -642,7 +642,10 @@ cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec
     if ((e = launch_dense_yz(m, true, P, spec, st)) != cudaSuccess) return e;
     mk(m == 1 ? "dense_y_fwd" : "dense_z_fwd");
   }
-  if (P.kind[2] == 0 && P.kind[1] != 2) {
+  if (P.kind[2] == 0 && P.kind[1] != 2 && P.zcyc) {
+    if ((e = launch_cyc_z_solve(P, spec, st)) != cudaSuccess) return e;
+    mk("cyc_z_solve");
+  } else if (P.kind[2] == 0 && P.kind[1] != 2) {
 #define Z_SOL(n) e = launch_z<(n)>(P, spec, c, st)
     NS_SIZE_SWITCH(P.nz, Z_SOL)
 #undef Z_SOL

@@ -202,6 +202,17 @@ struct FftPlan {
   double tri_elo, tri_ehi;  // end-row diagonal changes: pbc 2 -1, pbc 3 +1, pbc 4 0
   const double2* tri_m;   // the forward multipliers (re, im) of every line, laid out like the spectrum
                           // (launch_tri_table); read by the batched z solve (tri_lines_body)
+  // All-periodic boxes: the z stage as cyclic tridiagonal line solves (ns_cyclic.cu)
+  // instead of z FFT * 1/lambda * z IFFT.  Tables per (kx, ky) mode, laid out like the
+  // spectrum: T's multipliers, w = rs T^-1 e0, q = T^-1 u; per mode (1/c, SM denominator).
+  int zcyc;
+  const double* cyc_m;
+  const double* cyc_w;
+  const double* cyc_q;
+  const double2* cyc_s;
+  const double* cyc_v;    // the singular (0, 0) line's solution mean, as a functional of its data
+  double cyc_rs;          // h_z^2 * scale * nz
+  double cyc_h2;          // h_z^2
   double mod_lo[3], mod_hi[3];        // pr_bc_staggered_modify_rhs coefficients per axis
   const double* face_lo[3];           // pressure face planes per axis (internal slot order)
   const double* face_hi[3];
@@ -256,6 +267,12 @@ cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec
 // Symmetry bits of a dense transform pair of even size n (sym in FftPlan),
 // checked entry by entry on the host (ns_dct.cu).
 int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double>& G);
+// The cyclic z solve of an all-periodic plan (ns_cyclic.cu): the size of its
+// tables, their construction (sets P.cyc_*; eig_x, eig_o, cyc_h2, cyc_rs set
+// before), and the solve of every z line of the spectrum in place.
+size_t cyc_table_doubles(const FftPlan& P);
+cudaError_t launch_cyc_table(FftPlan& P, double* buf, cudaStream_t st);
+cudaError_t launch_cyc_z_solve(const FftPlan& P, double2* spec, cudaStream_t st);
 // Lanes per x line of the dense x passes: the next power of two at or above
 // nx/2 (the mode pairs of a line), at most 32; a 128-thread CTA takes 128/G lines.
 __host__ __device__ __forceinline__ int dense_x_group(int nx) {

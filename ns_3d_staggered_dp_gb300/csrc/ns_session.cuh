@@ -36,6 +36,7 @@ struct ns_handle {
   double* stage_f[7] = {};                     // ns_step_host: one staging buffer per state field
   std::vector<cudaEvent_t> ev_slab;            // ns_step_host: one event per z-slab
   double* inv_lam = nullptr;
+  double* cyc_buf = nullptr;  // tables of the cyclic z solve (all-periodic boxes)
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
   ns::FftPlan plan{};
   // ADI factors
