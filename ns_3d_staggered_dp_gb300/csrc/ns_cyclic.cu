@@ -110,10 +110,11 @@ __global__ void __launch_bounds__(CYC_T) cyc_table_kernel(FftPlan P, double* __r
 // One thread per z line (mode t): forward walk (Thomas with T's multipliers,
 // y[0] = w . R alongside), the Sherman-Morrison coefficient, backward walk
 // writing x = y - alpha q.
-__global__ void __launch_bounds__(CYC_T) cyc_solve_kernel(FftPlan P, double2* __restrict__ spec) {
+// SING: the singular line (t = 0), which ends by removing the mean of its
+// result; the other lines skip that subtraction.
+template <bool SING>
+__device__ __forceinline__ void cyc_walk(const FftPlan& P, double2* __restrict__ spec, int t) {
   const int S = P.nxh * P.ny;
-  const int t = blockIdx.x * CYC_T + threadIdx.x;
-  if (t >= S) return;
   const int n = P.nz;
   const double rs = P.cyc_rs;
   const double* __restrict__ M = P.cyc_m + t;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(CYC_T) cyc_solve_kernel(FftPlan P, double2* __
   // the singular line (t = 0) runs the same walk on its own tables and ends
   // by removing the mean of its result, beta = V . R (load-only pre-pass)
   double2 beta = make_double2(0.0, 0.0);
-  if (t == 0) {
+  if (SING) {
 #pragma unroll 8
     for (int j = 0; j < n; ++j) {
       const double2 r = g[(long long)j * S];
@@ -185,7 +186,9 @@ __global__ void __launch_bounds__(CYC_T) cyc_solve_kernel(FftPlan P, double2* __
   }
   {
     const double q = __ldg(Q + (long long)(n - 1) * S);
-    g[(long long)(n - 1) * S] = make_double2(fma(-ax, q, p.x) - beta.x, fma(-ay, q, p.y) - beta.y);
+    double2 x = make_double2(fma(-ax, q, p.x), fma(-ay, q, p.y));
+    if (SING) { x.x -= beta.x; x.y -= beta.y; }
+    g[(long long)(n - 1) * S] = x;
   }
   for (int j0 = n - 2; j0 >= 0; j0 -= PD) {
 #pragma unroll
@@ -202,12 +205,26 @@ __global__ void __launch_bounds__(CYC_T) cyc_solve_kernel(FftPlan P, double2* __
       if (j >= 0) {
         p.x = fma(-mb[q], p.x, rb[q].x);
         p.y = fma(-mb[q], p.y, rb[q].y);
-        g[(long long)j * S] = make_double2(fma(-ax, qb[q], p.x) - beta.x, fma(-ay, qb[q], p.y) - beta.y);
+        double2 x = make_double2(fma(-ax, qb[q], p.x), fma(-ay, qb[q], p.y));
+        if (SING) { x.x -= beta.x; x.y -= beta.y; }
+        g[(long long)j * S] = x;
       }
     }
 #pragma unroll
     for (int q = 0; q < PD; ++q) { rb[q] = rn[q]; mb[q] = mn[q]; qb[q] = qn[q]; }
   }
+}
+
+// Threads 0..S-2 take the lines 1..S-1; the singular line 0 goes to the
+// first thread of a warp of its own (a warp running both walks would take as
+// long as the two together).
+__host__ __device__ __forceinline__ int cyc_sing_thread(int S) { return (S - 1 + 31) / 32 * 32; }
+
+__global__ void __launch_bounds__(CYC_T) cyc_solve_kernel(FftPlan P, double2* __restrict__ spec) {
+  const int S = P.nxh * P.ny;
+  const int g = blockIdx.x * CYC_T + threadIdx.x;
+  if (g < S - 1) cyc_walk<false>(P, spec, g + 1);
+  else if (g == cyc_sing_thread(S)) cyc_walk<true>(P, spec, 0);
 }
 
 }  // namespace
@@ -234,8 +251,8 @@ cudaError_t launch_cyc_table(FftPlan& P, double* buf, cudaStream_t st) {
 }
 
 cudaError_t launch_cyc_z_solve(const FftPlan& P, double2* spec, cudaStream_t st) {
-  const size_t S = (size_t)P.nxh * P.ny;
-  cyc_solve_kernel<<<(unsigned)((S + CYC_T - 1) / CYC_T), CYC_T, 0, st>>>(P, spec);
+  const int threads = cyc_sing_thread(P.nxh * P.ny) + 1;
+  cyc_solve_kernel<<<(unsigned)((threads + CYC_T - 1) / CYC_T), CYC_T, 0, st>>>(P, spec);
   return cudaGetLastError();
 }
 
