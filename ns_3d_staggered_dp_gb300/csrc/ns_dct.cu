@@ -78,6 +78,47 @@ __device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArg
         r[nx - 1 - n] = a0 - b0;
       }
     __syncwarp();
+    const int lv1 = (S.sym[0] >> 2) & 3;  // bit p: the modes of parity p fold once more
+    if (lv1 == 1 || lv1 == 2) {
+      // Second fold of one branch over its H points (sign (-1)^((k >> 1) & 1)):
+      // the even branch s (at 0..H-1) into s2 at n and d2 at H-1-n, the odd
+      // branch d (d[n] at N-1-n) into s2 at N-1-n and d2 at H+n, n < H/2.
+      // The folded mode of a pair then sums H/2 terms, the other one sums
+      // the mirrored terms n and H-1-n together.
+      const int Q = H / 2;
+      if (valid)
+        for (int n = gl; n < Q; n += G) {
+          const int ia = lv1 == 1 ? n : nx - 1 - n, ib = lv1 == 1 ? H - 1 - n : H + n;
+          const double a0 = r[ia], b0 = r[ib];
+          r[ia] = a0 + b0;
+          r[ib] = a0 - b0;
+        }
+      __syncwarp();
+      if (!valid) return;
+      for (int q = gl; q < H; q += G) {
+        const int b1 = q & 1;  // ((2q or 2q+1) >> 1) & 1
+        double a = 0.0, b = 0.0;
+        if (lv1 == 1) {  // mode 2q folded, mode 2q+1 on d
+          for (int n = 0; n < Q; ++n) {
+            const double2 f = *reinterpret_cast<const double2*>(FT + (long long)n * nx + 2 * q);
+            const double fm = FT[(long long)(H - 1 - n) * nx + 2 * q + 1];
+            a = fma(f.x, b1 ? r[H - 1 - n] : r[n], a);
+            b = fma(f.y, r[nx - 1 - n], b);
+            b = fma(fm, r[H + n], b);
+          }
+        } else {  // mode 2q on s, mode 2q+1 folded
+          for (int n = 0; n < Q; ++n) {
+            const double2 f = *reinterpret_cast<const double2*>(FT + (long long)n * nx + 2 * q);
+            const double fm = FT[(long long)(H - 1 - n) * nx + 2 * q];
+            a = fma(f.x, r[n], a);
+            a = fma(fm, r[H - 1 - n], a);
+            b = fma(f.y, b1 ? r[H + n] : r[nx - 1 - n], b);
+          }
+        }
+        out[q] = make_double2(a, b);
+      }
+      return;
+    }
     if (!valid) return;
     for (int q = gl; q < H; q += G) {
       double a = 0.0, b = 0.0;
@@ -178,6 +219,58 @@ __device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __rest
         line[(N - 1 - n) * LPC] = make_double2(a.x - b.x, a.y - b.y);
       }
     __syncthreads();
+    const int lv1 = (S.sym[AXIS] >> 2) & 3;  // bit p: the modes of parity p fold once more
+    if (lv1 == 1 || lv1 == 2) {
+      // Second fold of branch p over its H points (sign (-1)^((k >> 1) & 1)):
+      // the even branch s (at 0..H-1) into s2 at q and d2 at H-1-q, the odd
+      // branch d (d[q] at N-1-q) into s2 at N-1-q and d2 at H+q, q < H/2.
+      const int Q = H / 2, pf = lv1 == 1 ? 0 : 1;
+      if (valid)
+        for (int q = t; q < Q; q += T) {
+          const int ia = pf ? N - 1 - q : q, ib = pf ? H + q : H - 1 - q;
+          const double2 a = line[ia * LPC], b = line[ib * LPC];
+          line[ia * LPC] = make_double2(a.x + b.x, a.y + b.y);
+          line[ib * LPC] = make_double2(a.x - b.x, a.y - b.y);
+        }
+      __syncthreads();
+      if (!valid) return;
+      // each thread takes modes 2m + pu (H terms) and 2m + pf (H/2 terms) for
+      // m = t, t + T, ..., so every thread has the same loop lengths
+      const int pu = 1 - pf;
+      for (int m = t; m < H; m += T) {
+        {
+          const int kk = 2 * m + pu;
+          const double2* src = pu ? line + (long long)(N - 1) * LPC : line;
+          const int step = pu ? -LPC : LPC;
+          const double* __restrict__ row = M + (long long)kk * N;
+          double2 acc = make_double2(0.0, 0.0);
+          for (int n = 0; n < H; ++n) {
+            const double2 v = src[n * step];
+            const double mm = __ldg(row + n);
+            acc.x = fma(mm, v.x, acc.x);
+            acc.y = fma(mm, v.y, acc.y);
+          }
+          g[(long long)kk * st] = acc;
+        }
+        {
+          const int kk = 2 * m + pf, b1 = m & 1;  // (kk >> 1) & 1
+          const double2* src;
+          int step;
+          if (pf == 0) { src = b1 ? line + (long long)(H - 1) * LPC : line; step = b1 ? -LPC : LPC; }
+          else { src = b1 ? line + (long long)H * LPC : line + (long long)(N - 1) * LPC; step = b1 ? LPC : -LPC; }
+          const double* __restrict__ row = M + (long long)kk * N;
+          double2 acc = make_double2(0.0, 0.0);
+          for (int n = 0; n < Q; ++n) {
+            const double2 v = src[n * step];
+            const double mm = __ldg(row + n);
+            acc.x = fma(mm, v.x, acc.x);
+            acc.y = fma(mm, v.y, acc.y);
+          }
+          g[(long long)kk * st] = acc;
+        }
+      }
+      return;
+    }
     if (!valid) return;
     for (int kk = t; kk < N; kk += T) {  // kk has the parity of t
       const double2* src = (kk & 1) ? line + (long long)(N - 1) * LPC : line;
@@ -542,7 +635,24 @@ int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double
       if (std::fabs(F[(size_t)r * n + (n - 1 - q)] - sg_r * F[(size_t)r * n + q]) > 4e-16 * fm) fs = false;
       if (std::fabs(G[(size_t)(n - 1 - r) * n + q] - sg_q * G[(size_t)r * n + q]) > 4e-16 * gm) gs = false;
     }
-  return (fs ? 1 : 0) | (gs ? 2 : 0);
+  int bits = (fs ? 1 : 0) | (gs ? 2 : 0);
+  // Second level: within the modes of one parity, over the first H = n/2
+  // points, F[k][H-1-q] = s_k F[k][q] and G[H-1-q][k] = s_k G[q][k] with
+  // s_k = (-1)^((k >> 1) & 1).  DCT-II has it on its even modes (a half-size
+  // DCT-II), DST-II on its odd ones.
+  const int H = n / 2;
+  if (H % 2 == 0) {
+    bool f1[2] = {fs, fs}, g1[2] = {gs, gs};
+    for (int k = 0; k < n; ++k) {
+      const double sg = ((k >> 1) & 1) ? -1.0 : 1.0;
+      for (int q = 0; q < H; ++q) {
+        if (std::fabs(F[(size_t)k * n + (H - 1 - q)] - sg * F[(size_t)k * n + q]) > 4e-16 * fm) f1[k & 1] = false;
+        if (std::fabs(G[(size_t)(H - 1 - q) * n + k] - sg * G[(size_t)q * n + k]) > 4e-16 * gm) g1[k & 1] = false;
+      }
+    }
+    bits |= (f1[0] ? 4 : 0) | (f1[1] ? 8 : 0) | (g1[0] ? 16 : 0) | (g1[1] ? 32 : 0);
+  }
+  return bits;
 }
 
 cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st) {
