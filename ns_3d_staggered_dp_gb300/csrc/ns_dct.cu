@@ -146,7 +146,7 @@ __device__ __forceinline__ void dense_x_fwd_body(const SpecPlan& S, const DivArg
 // x inverse for a non-periodic x axis: packed modes -> G_x -> dp slots 1..nx.
 __device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double2* __restrict__ spec, double* dp,
                                                  const Layout& L, double* xs, int bx) {
-  const int G = dense_x_group(S.nx);
+  const int G = dense_x_inv_group(S.sym[0], S.nx);
   const int grp = threadIdx.x / G, gl = threadIdx.x % G;
   const int line = bx * (128 / G) + grp;
   const int nx = S.nx, ny = S.ny, nz = S.nz;
@@ -164,6 +164,36 @@ __device__ __forceinline__ void dense_x_inv_body(const SpecPlan& S, const double
   if (!valid) return;
   const double* __restrict__ GT = S.inv[0];  // G^T: GT[kk * N + n] = G[n][kk] (x = G X)
   double* o = dp + L.at(1, j, k);
+  const int lvi = (S.sym[0] >> 4) & 3;  // bit p: the columns of parity p fold once more
+  if ((S.sym[0] & 2) && (lvi == 1 || lvi == 2)) {
+    // Row pairs (n, H-1-n), n < H/2: G[H-1-n][k] = (-1)^((k >> 1) & 1) G[n][k]
+    // on the columns of parity pf, so their partial sums F0 (k = pf mod 4)
+    // and F1 (k = pf + 2 mod 4) give both rows as F0 + F1 and F0 - F1; the
+    // other parity is summed for both rows.  Then out[r] = E_r + O_r and
+    // out[N-1-r] = E_r - O_r for r = n and H-1-n.
+    const int H = nx / 2, Q = H / 2, pf = lvi == 1 ? 0 : 1, pu = 1 - pf;
+    for (int n = gl; n < Q; n += G) {
+      const int m = H - 1 - n;
+      double f0 = 0.0, f1 = 0.0, un = 0.0, um = 0.0;
+      for (int c = 0; c < nx; c += 4) {
+        const double x0 = X[c + pf], x1 = X[c + pf + 2], y0 = X[c + pu], y1 = X[c + pu + 2];
+        f0 = fma(__ldg(GT + (long long)(c + pf) * nx + n), x0, f0);
+        f1 = fma(__ldg(GT + (long long)(c + pf + 2) * nx + n), x1, f1);
+        un = fma(__ldg(GT + (long long)(c + pu) * nx + n), y0, un);
+        un = fma(__ldg(GT + (long long)(c + pu + 2) * nx + n), y1, un);
+        um = fma(__ldg(GT + (long long)(c + pu) * nx + m), y0, um);
+        um = fma(__ldg(GT + (long long)(c + pu + 2) * nx + m), y1, um);
+      }
+      const double fn = f0 + f1, fm = f0 - f1;
+      const double en = pf ? un : fn, on = pf ? fn : un;  // even and odd sums of row n
+      const double em = pf ? um : fm, om = pf ? fm : um;  // and of row m
+      o[n] = en + on;
+      o[nx - 1 - n] = en - on;
+      o[m] = em + om;
+      o[nx - 1 - m] = em - om;
+    }
+    return;
+  }
   if (S.sym[0] & 2) {
     // G[N-1-n][k] = (-1)^k G[n][k]: out[n] = E + O, out[N-1-n] = E - O
     for (int n = gl; n < nx / 2; n += G) {
@@ -579,7 +609,7 @@ __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __
 void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
   gy = 1;
   if (pass == 0 || pass == 1) {
-    const int per = 128 / dense_x_group(S.nx);
+    const int per = 128 / (pass == 0 ? dense_x_group(S.nx) : dense_x_inv_group(S.sym[0], S.nx));
     gx = (S.ny * S.nz + per - 1) / per;
   }
   else if (pass == 2 || pass == 3) gx = (S.nxs * S.nz + 15) / 16;  // dense_yz_body: 16 lines per item
@@ -587,7 +617,8 @@ void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
 }
 
 size_t spec_pass_smem(int pass, const SpecPlan& S) {
-  if (pass == 0 || pass == 1) return (size_t)(128 / dense_x_group(S.nx)) * S.nx * sizeof(double);
+  if (pass == 0) return (size_t)(128 / dense_x_group(S.nx)) * S.nx * sizeof(double);
+  if (pass == 1) return (size_t)(128 / dense_x_inv_group(S.sym[0], S.nx)) * S.nx * sizeof(double);
   if (pass == 2 || pass == 3) return (size_t)S.ny * 16 * sizeof(double2);
   return (size_t)S.nz * TRI_T * sizeof(double) * 2;
 }
@@ -616,7 +647,7 @@ cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchIte
 
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                            cudaStream_t st) {
-  const int lines = S.ny * S.nz, per = 128 / dense_x_group(S.nx);
+  const int lines = S.ny * S.nz, per = 128 / (fwd ? dense_x_group(S.nx) : dense_x_inv_group(S.sym[0], S.nx));
   const size_t sm = (size_t)per * S.nx * sizeof(double);
   if (fwd) dense_x_fwd_kernel<<<(lines + per - 1) / per, 128, sm, st>>>(S, d, spec);
   else dense_x_inv_kernel<<<(lines + per - 1) / per, 128, sm, st>>>(S, spec, dp, L);

@@ -281,6 +281,12 @@ __host__ __device__ __forceinline__ int dense_x_group(int nx) {
   while (g < h && g < 32) g <<= 1;
   return g;
 }
+// The x inverse takes row pairs (n, H-1-n) when its matrix folds twice
+// (sym bits 1 and 4 or 5), so its groups cover nx/4 lanes.
+__host__ __device__ __forceinline__ int dense_x_inv_group(const int sym, const int nx) {
+  const int lvi = (sym >> 4) & 3;
+  return ((sym & 2) && (lvi == 1 || lvi == 2)) ? dense_x_group(nx / 2) : dense_x_group(nx);
+}
 // Dense passes (ns_dct.cu): x forward/inverse, y/z forward/inverse.
 cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                            cudaStream_t st);
