@@ -317,6 +317,49 @@ __device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __rest
     }
     return;
   }
+  const int lvi = (S.sym[AXIS] >> 4) & 3;  // bit p: the columns of parity p fold once more
+  if (sym && (lvi == 1 || lvi == 2) && N % 8 == 0) {
+    // Row pairs (n, H-1-n), n < H/2, from the second fold of the columns of
+    // parity pf (see dense_x_inv_body).  The two threads t and t^1 of a pair
+    // (lanes 16 apart) take one half of the columns each and add their sums
+    // by shuffle; every lane stays in the loop for the shuffles.
+    const int H = N / 2, Q = H / 2, pf = lvi == 1 ? 0 : 1, pu = 1 - pf;
+    const int half = t & 1, pr = t >> 1;
+    const int c0 = half ? H : 0, c1 = half ? N : H;
+    for (int n = pr; n < Q; n += T / 2) {
+      const int m = H - 1 - n;
+      const double* __restrict__ rn = M + (long long)n * N;
+      const double* __restrict__ rm = M + (long long)m * N;
+      double2 f0 = make_double2(0.0, 0.0), f1 = f0, un = f0, um = f0;
+      for (int c = c0; c < c1; c += 4) {
+        const double2 x0 = line[(c + pf) * LPC], x1 = line[(c + pf + 2) * LPC];
+        const double2 y0 = line[(c + pu) * LPC], y1 = line[(c + pu + 2) * LPC];
+        const double a0 = __ldg(rn + c + pf), a1 = __ldg(rn + c + pf + 2);
+        const double b0 = __ldg(rn + c + pu), b1 = __ldg(rn + c + pu + 2);
+        const double e0 = __ldg(rm + c + pu), e1 = __ldg(rm + c + pu + 2);
+        f0.x = fma(a0, x0.x, f0.x); f0.y = fma(a0, x0.y, f0.y);
+        f1.x = fma(a1, x1.x, f1.x); f1.y = fma(a1, x1.y, f1.y);
+        un.x = fma(b0, y0.x, un.x); un.y = fma(b0, y0.y, un.y);
+        un.x = fma(b1, y1.x, un.x); un.y = fma(b1, y1.y, un.y);
+        um.x = fma(e0, y0.x, um.x); um.y = fma(e0, y0.y, um.y);
+        um.x = fma(e1, y1.x, um.x); um.y = fma(e1, y1.y, um.y);
+      }
+      f0.x += __shfl_xor_sync(0xffffffffu, f0.x, 16); f0.y += __shfl_xor_sync(0xffffffffu, f0.y, 16);
+      f1.x += __shfl_xor_sync(0xffffffffu, f1.x, 16); f1.y += __shfl_xor_sync(0xffffffffu, f1.y, 16);
+      un.x += __shfl_xor_sync(0xffffffffu, un.x, 16); un.y += __shfl_xor_sync(0xffffffffu, un.y, 16);
+      um.x += __shfl_xor_sync(0xffffffffu, um.x, 16); um.y += __shfl_xor_sync(0xffffffffu, um.y, 16);
+      if (valid && half == 0) {
+        const double2 fn = make_double2(f0.x + f1.x, f0.y + f1.y), fm = make_double2(f0.x - f1.x, f0.y - f1.y);
+        const double2 en = pf ? un : fn, on = pf ? fn : un;  // even and odd sums of row n
+        const double2 em = pf ? um : fm, om = pf ? fm : um;  // and of row m
+        g[(long long)n * st] = make_double2(en.x + on.x, en.y + on.y);
+        g[(long long)(N - 1 - n) * st] = make_double2(en.x - on.x, en.y - on.y);
+        g[(long long)m * st] = make_double2(em.x + om.x, em.y + om.y);
+        g[(long long)(N - 1 - m) * st] = make_double2(em.x - om.x, em.y - om.y);
+      }
+    }
+    return;
+  }
   if (sym) {
     // G[N-1-n][k] = (-1)^k G[n][k]: even and odd partial sums of row n give
     // out[n] = E + O and out[N-1-n] = E - O
