@@ -274,7 +274,8 @@ cudaError_t ensure_xfer(ns_handle* h) {
   if ((e = cudaStreamCreateWithFlags(&h->xfer, cudaStreamNonBlocking)) != cudaSuccess) return e;
   int least = 0, greatest = 0;
   if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess) return e;
-  if ((e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, least)) != cudaSuccess) return e;
+  (void)least;
+  if ((e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
   if ((e = cudaStreamCreateWithPriority(&h->prio, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
   for (int b = 0; b < 2; ++b) {
     if ((e = cudaEventCreateWithFlags(&h->ev_full[b], cudaEventDisableTiming)) != cudaSuccess) return e;
@@ -1193,9 +1194,12 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     NS_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     h->ev_slab.push_back(e);
   }
-  // The compute runs on the handle's greatest-priority stream (after the
-  // caller's stream): the predictor chain keeps pace with the copies, and the
-  // x and y sweeps on the lowest-priority side stream take the SMs it leaves.
+  // The compute runs on two greatest-priority streams of the handle (after
+  // the caller's stream): the predictor chain on one, the x and y sweeps of
+  // each finished slab beside it on the other, ahead of any other work on the
+  // device.  (With the sweeps at the lowest priority they fell a slab behind;
+  // in line after the predictor, the slab's sliced sweeps made the chain as
+  // slow as the copies.)
   trace_mark(h, h->stream, "start");
   NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_start], h->stream));
   NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[ev_start], 0));

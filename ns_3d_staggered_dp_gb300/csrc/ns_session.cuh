@@ -29,7 +29,7 @@ struct ns_handle {
   double* stage = nullptr;   // host<->device staging of one reference-shaped field
   double* stage2 = nullptr;  // second staging buffer (multi-field transfers)
   cudaStream_t xfer = nullptr;  // copy stream of the multi-field transfers
-  cudaStream_t side = nullptr;  // second compute stream of ns_step_host (x and y sweeps of a slab), lowest priority
+  cudaStream_t side = nullptr;  // second compute stream of ns_step_host (x and y sweeps of a slab), greatest priority
   cudaStream_t prio = nullptr;  // compute stream of ns_step_host, greatest priority
   cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   cudaEvent_t ev_aux[2] = {nullptr, nullptr};  // ns_step_host: history final, step done
