@@ -238,6 +238,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device="cuda"):
+    """The largest x over all ranks (the slowest replica sets the job's time)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, seconds):
+    """Whole-job throughput of `world` replicas that each did units_per_rank
+    in `seconds` (the max over ranks)."""
+    return world * units_per_rank / seconds
+
+
 def workload(name, n):
     """Grid, initial state, step parameters and JSON config of a workload."""
     if name == "channel":
@@ -640,15 +657,10 @@ def run_ours(args):
             e1.record(stream)
             torch.cuda.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
+        ms = max_over_ranks(e0.elapsed_time(e1), world)
         launches = s.launch_count() - l0
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
         ms_per_step = ms / args.steps
-        value = world * ncell * args.steps / (ms / 1e3)
+        value = job_rate(world, ncell * args.steps, ms / 1e3)
         d = s.diag()
 
         # ---- per-kernel times (events between launches, eager) ----
@@ -704,7 +716,8 @@ def run_ours(args):
         e2e_phases = {"set_state_ms": 1e3 * (tp[1] - tp[0]), "step_ms": 1e3 * (tp[2] - tp[1]),
                       "get_state_ms": 1e3 * (tp[3] - tp[2])}
         barrier()
-        e2e_value = world * ncell * e2e_steps / e2e_sec
+        e2e_sec = max_over_ranks(e2e_sec, world)
+        e2e_value = job_rate(world, ncell * e2e_steps, e2e_sec)
 
     if rank != 0:
         return 0
