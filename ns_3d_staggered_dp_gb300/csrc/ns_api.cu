@@ -527,6 +527,7 @@ PredictArgs predict_args(ns_handle* h) {
   a.u = h->u; a.v = h->v; a.w = h->w; a.p = h->p;
   a.us = h->us; a.vs = h->vs; a.ws = h->ws;
   a.hx = h->hx; a.hy = h->hy; a.hz = h->hz;
+  a.err = h->dev_err;
   set_predict_coeffs(a, c.bc, h->dx, h->dy, h->dz, c.dt, c.nu);
   return a;
 }
@@ -635,7 +636,7 @@ int enqueue_tail(ns_handle* h, bool adi_xy_done);
 int enqueue_step(ns_handle* h, bool first, cudaEvent_t after_predict = nullptr) {
   const ns_config& c = h->cfg;
   PredictArgs a = predict_args(h);
-  NS_CUDA(h, launch_predict(a, c.scheme, first, c.dp_flag != 0, 0, h->stream));
+  NS_CUDA(h, launch_predict(a, c.scheme, first, c.dp_flag != 0, 0, h->stream, &h->tma));
   mark(h, "predict");
   if (after_predict) NS_CUDA(h, cudaEventRecord(after_predict, h->stream));
   return enqueue_tail(h, false);
@@ -966,6 +967,7 @@ void free_all(ns_handle* h) {
   for (cudaEvent_t e : h->trace_pool) cudaEventDestroy(e);
   if (h->tw) cudaFree(h->tw);
   if (h->diag_bits) cudaFree(h->diag_bits);
+  if (h->dev_err) cudaFree(h->dev_err);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
 }
@@ -1053,6 +1055,12 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
       for (int f = 0; f < 4; ++f)
         for (int d = 0; d < 2; ++d) h->faces[set].ax[a].f[f][d] = h->face_buf + face_offset(h->L, set, a, f, d);
   if (cudaMalloc(&h->diag_bits, sizeof(unsigned long long)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+  if (cudaMalloc(&h->dev_err, sizeof(int)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+  if (cudaMemsetAsync(h->dev_err, 0, sizeof(int), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+  // without the driver's map encoder (or with NS_PREDICT_TMA=0 in the environment)
+  // the predictor stages its tiles with cp.async; the results are the same bits
+  const char* tma_env = std::getenv("NS_PREDICT_TMA");
+  if (!(tma_env && tma_env[0] == '0')) ns::make_pred_tma(h->tma, h->L, h->u, h->v, h->w);
   if ((s = build_plans(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
   if ((s = build_adi(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
@@ -1278,7 +1286,7 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     const int e = hi >= nz + 2 ? nz + 1 : std::min(nz + 1, hi - 2);
     if (e > pred_done) {
       const int kc = std::max(2, std::min(KC, (e - pred_done) / 4));
-      NS_CUDA(h, launch_predict_planes(pa, c.scheme, first, c.dp_flag != 0, pred_done, e, kc, h->stream));
+      NS_CUDA(h, launch_predict_planes(pa, c.scheme, first, c.dp_flag != 0, pred_done, e, kc, h->stream, &h->tma));
       mark(h, "predict");
       trace_mark(h, h->stream, "predict", s, lo, hi);
       pred_done = e;
@@ -1460,6 +1468,8 @@ int ns_get_diag(ns_handle* h, ns_diag* d) {
   // u(nx/2, ny/2, nz/2) in Fortran indices -> slot (nx/2, ny/2-1, nz/2-1)
   const long long g = h->L.at(c.nx / 2, c.ny / 2 - 1, c.nz / 2 - 1);
   NS_CUDA(h, cudaMemcpyAsync(&probe, h->u + g, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  int timed_out = 0;
+  NS_CUDA(h, cudaMemcpyAsync(&timed_out, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
   double md;
   std::memcpy(&md, &bits, sizeof(md));
@@ -1468,6 +1478,7 @@ int ns_get_diag(ns_handle* h, ns_diag* d) {
   d->steps_done = h->steps;
   d->euler_start_pending = h->first_pending ? 1 : 0;
   d->reserved = 0;
+  if (timed_out) return fail(h, NS_ERR_TIMEOUT, "a tile-loader wait of the predictor gave up; the state is invalid");
   if (!std::isfinite(md)) return fail(h, NS_ERR_NONFINITE, "non-finite divergence");
   return NS_OK;
 }

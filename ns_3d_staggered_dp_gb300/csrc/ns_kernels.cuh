@@ -1,5 +1,6 @@
 // Kernel argument blocks and launchers of the FP64 staggered step.
 #pragma once
+#include <cuda.h>
 #include <vector>
 
 #include "ns_internal.cuh"
@@ -51,7 +52,19 @@ struct PredictArgs {
   // Plane ranges with their own chunk depth (0: the defaults): chunk bz holds
   // the planes 1 + koff + kc*bz .. up to kend (exclusive; 0: nz + 1).
   int kc, koff, kend;
+  int* err;  // device word set to 1 when a bounded wait of the tile loader gave up (may be null)
 };
+// Tile-loader maps (TMA) of three fields of one layout for the session
+// predictor (ns_predict.cu): 3D tensors (px, ny+2, nz+2) of doubles, boxes of
+// 40 x 18 x 1.  Used when the predictor's u, v, w are the mapped fields.
+struct PredTma {
+  CUtensorMap u, v, w;
+  const double* pu;
+  const double* pv;
+  const double* pw;
+  int ready;
+};
+bool make_pred_tma(PredTma& t, const Layout& L, const double* u, const double* v, const double* w);
 
 // Combine the stencil pieces into u* and rewrite the AB2 history at g.
 template <int SCHEME, bool FIRST>
@@ -85,13 +98,14 @@ __device__ __forceinline__ double predictor_combine(const PredictArgs& a, const 
 }
 
 size_t predict_smem_bytes();
-cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st);
+cudaError_t launch_predict(const PredictArgs& a, int scheme, bool first, bool dpf, int mode, cudaStream_t st,
+                           const PredTma* tma = nullptr);
 int predict_chunk_planes();
 // The predictor on the cell planes [p0, p1) (1 <= p0 < p1 <= nz + 1) in
 // chunks of kc planes per CTA: small chunks spread a short range over more
 // CTAs (less latency, a little more work per plane).
 cudaError_t launch_predict_planes(PredictArgs a, int scheme, bool first, bool dpf, int p0, int p1, int kc,
-                                  cudaStream_t st);
+                                  cudaStream_t st, const PredTma* tma = nullptr);
 // Predictor tiles of one box (work items of the batched launch).
 void predict_tiles(const Layout& L, int& gx, int& gy, int& gz);
 // Batched predictor over the items (grid <= 0: one wave of resident CTAs).

@@ -47,6 +47,8 @@ struct ns_handle {
   ns::FaceSet faces[4]{};
   bool face_set_nonzero[4] = {false, false, false, false};
   unsigned long long* diag_bits = nullptr;
+  int* dev_err = nullptr;  // set on the device when a bounded wait of the predictor's tile loader gave up
+  ns::PredTma tma{};        // tile-loader maps of u, v, w (tma.ready = 0: the predictor loads tiles itself)
   // state
   bool first_pending = true;
   long long steps = 0;

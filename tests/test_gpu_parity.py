@@ -257,3 +257,35 @@ def test_nonfinite_state_is_reported():
         s.set_state(st.u, st.v, st.w, st.p)  # the same handle runs a clean step afterwards
         s.step(1)
         assert s.diag()["max_div"] < 1e-10
+
+
+@pytest.mark.parametrize("case", [
+    ((16, 16, 16), {}),                                  # one x tile, partly filled
+    ((32, 16, 64), {"scheme": O.AB2, "dp_flag": 1}),
+    ((48, 40, 24), {"bc": (2, 2, 2), "pbc": (3, 3, 3)}),  # ragged x and y tiles, walls everywhere
+    ((64, 32, 32), {"bc": (1, 1, 2), "pbc": (1, 1, 3), "dp_flag": 1}),
+])
+def test_predictor_tile_loaders_agree(case, monkeypatch):
+    """The predictor stages its tiles with the tensor-memory-access loader
+    (cp.async.bulk.tensor into an mbarrier ring) unless NS_PREDICT_TMA=0 at
+    ns_create selects the cp.async loader: both give the same bits, for the
+    device-resident step and for ns_step_host, on full and ragged tiles."""
+    n, kw = case
+    kw = dict(kw)
+    scheme = kw.pop("scheme", O.AB2_CN)
+    cfg = O.Config(*n, nu=0.02, dt=0.01, scheme=scheme, **kw)
+    st = random_state(cfg, 57, history=True)
+    hist = (st.px, st.py, st.pz)
+    res = []
+    for env in ("1", "0"):
+        monkeypatch.setenv("NS_PREDICT_TMA", env)
+        with session(cfg) as s:
+            s.set_state(st.u, st.v, st.w, st.p, hist)
+            s.step(2)
+            dev = s.get_state()
+            host = s.step_host(st.u, st.v, st.w, st.p, hist)
+            assert s.diag()["max_div"] < DIV_TOL
+        res.append((dev, host))
+    for a, b in zip(res[0], res[1]):
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
