@@ -277,6 +277,7 @@ cudaError_t ensure_xfer(ns_handle* h) {
   (void)least;
   if ((e = cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
   if ((e = cudaStreamCreateWithPriority(&h->prio, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
+  if ((e = cudaStreamCreateWithPriority(&h->scat, cudaStreamNonBlocking, greatest)) != cudaSuccess) return e;
   for (int b = 0; b < 2; ++b) {
     if ((e = cudaEventCreateWithFlags(&h->ev_full[b], cudaEventDisableTiming)) != cudaSuccess) return e;
     if ((e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming)) != cudaSuccess) return e;
@@ -956,6 +957,7 @@ void free_all(ns_handle* h) {
   if (h->xfer) cudaStreamDestroy(h->xfer);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->prio) cudaStreamDestroy(h->prio);
+  if (h->scat) cudaStreamDestroy(h->scat);
   for (int b = 0; b < 2; ++b) {
     if (h->ev_full[b]) cudaEventDestroy(h->ev_full[b]);
     if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
@@ -1194,10 +1196,11 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   while (tb.back() < nz + 2) tb.push_back(std::min(nz + 2, tb.back() + S));
   const int ntail = (int)tb.size() - 1;
   // events: front slabs (copy done), start, history out (3 per front slab),
-  // state out (4 per tail slab), predictor done (per front slab), sweeps done
+  // state out (4 per tail slab), predictor done (per front slab), sweeps
+  // done, the periodic-image prelude done, scatter done (per front slab)
   const int ev_start = nslab, ev_hist = nslab + 1, ev_tail = ev_hist + 3 * nslab, ev_pred = ev_tail + 4 * ntail;
-  const int ev_sweeps = ev_pred + nslab;
-  while ((int)h->ev_slab.size() < ev_sweeps + 1) {
+  const int ev_sweeps = ev_pred + nslab, ev_pre = ev_sweeps + 1, ev_scat = ev_pre + 1;
+  while ((int)h->ev_slab.size() < ev_scat + nslab) {
     cudaEvent_t e;
     NS_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     h->ev_slab.push_back(e);
@@ -1212,6 +1215,7 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_start], h->stream));
   NS_CUDA(h, cudaStreamWaitEvent(h->xfer, h->ev_slab[ev_start], 0));
   NS_CUDA(h, cudaStreamWaitEvent(h->prio, h->ev_slab[ev_start], 0));
+  NS_CUDA(h, cudaStreamWaitEvent(h->scat, h->ev_slab[ev_start], 0));
   struct StreamSwap {
     ns_handle* h;
     cudaStream_t saved;
@@ -1249,6 +1253,9 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     NS_CUDA(h, pack_launch(h, h->w, h->stage_f[2], 2, true, nullptr, nullptr, nullptr, nz - 1, nz));
     const int zonly[3] = {0, 0, 1};
     NS_CUDA(h, launch_extra_slots(L, h->u, h->v, h->w, zonly, h->stream));
+    // the last slab's scatter rewrites slot nz (same bits) after this read of it
+    NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_pre], h->stream));
+    NS_CUDA(h, cudaStreamWaitEvent(h->scat, h->ev_slab[ev_pre], 0));
   }
   for (int s = 0; s < nslab; ++s) {
     const int lo = fb[s], hi = fb[s + 1];
@@ -1264,21 +1271,31 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   const bool first = !hist && c.scheme != NS_EULER;
   int pred_done = 1, xy_done = 0, hist_done = 0;  // next cell plane to predict; slots swept / sent out
   PredictArgs pa = predict_args(h);
+  // Every slab is scattered into the padded layout on its own stream as soon
+  // as it lands: the scatter writes slots [lo, hi) only, above every plane
+  // the previous slab's predictor launch reads (its prefetch stops at slot
+  // hi_prev - 1) and the planes whose history is being sent out, so it runs
+  // beside that launch instead of queueing behind it.
   for (int s = 0; s < nslab; ++s) {
     const int lo = fb[s], hi = fb[s + 1];
-    NS_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_slab[s], 0));
+    NS_CUDA(h, cudaStreamWaitEvent(h->scat, h->ev_slab[s], 0));
     for (const In& f : in) {
       int r0, r1;
       ref_range(f, lo, hi, r0, r1);
-      NS_CUDA(h, pack_launch(h, f.dev, h->stage_f[f.q], f.fid, true, nullptr, nullptr, nullptr, r0, r1));
+      NS_CUDA(h, pack_launch(h, f.dev, h->stage_f[f.q], f.fid, true, nullptr, nullptr, h->scat, r0, r1));
     }
     {
       const long long n = (long long)(hi - lo) * (L.nx + L.ny + 4);
-      extra_xy_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 1024), 256, 0, h->stream>>>(
+      extra_xy_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 1024), 256, 0, h->scat>>>(
           L, h->u, h->v, c.bc[0] == 1, c.bc[1] == 1, lo, hi);
       NS_CUDA(h, cudaGetLastError());
     }
-    trace_mark(h, h->stream, "scatter", s, lo, hi);
+    NS_CUDA(h, cudaEventRecord(h->ev_slab[ev_scat + s], h->scat));
+    trace_mark(h, h->scat, "scatter", s, lo, hi);
+  }
+  for (int s = 0; s < nslab; ++s) {
+    const int lo = fb[s], hi = fb[s + 1];
+    NS_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_slab[ev_scat + s], 0));
     // cell planes whose stencil and the two planes above it (read by the
     // prefetch) have arrived; a quarter of the range per CTA, at most
     // KC planes: short ranges at the top spread over as many CTAs as a

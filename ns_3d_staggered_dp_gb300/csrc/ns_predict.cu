@@ -371,8 +371,8 @@ template <int SCHEME, bool FIRST, bool DPF>
 __global__ void __launch_bounds__(TX*(TY + 1)) predict_tma_kernel(PredictArgs a, const __grid_constant__ CUtensorMap mu,
                                                                   const __grid_constant__ CUtensorMap mv,
                                                                   const __grid_constant__ CUtensorMap mw) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned char* p = smem_raw + ((128u - (sm_addr(smem_raw) & 127u)) & 127u);
+  extern __shared__ __align__(16) unsigned char smem_tma[];  // base rounded up to 128 B below
+  unsigned char* p = smem_tma + ((128u - (sm_addr(smem_tma) & 127u)) & 127u);
   predict_body<SCHEME, FIRST, DPF, 0, true>(a, *reinterpret_cast<PredSmem*>(p), blockIdx.x, blockIdx.y, blockIdx.z,
                                             &mu, &mv, &mw);
 }

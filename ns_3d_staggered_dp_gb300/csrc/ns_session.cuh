@@ -31,6 +31,7 @@ struct ns_handle {
   cudaStream_t xfer = nullptr;  // copy stream of the multi-field transfers
   cudaStream_t side = nullptr;  // second compute stream of ns_step_host (x and y sweeps of a slab), greatest priority
   cudaStream_t prio = nullptr;  // compute stream of ns_step_host, greatest priority
+  cudaStream_t scat = nullptr;  // ns_step_host: scatter of each landed slab into the padded layout, greatest priority
   cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   cudaEvent_t ev_aux[2] = {nullptr, nullptr};  // ns_step_host: history final, step done
   double* stage_f[7] = {};                     // ns_step_host: one staging buffer per state field
