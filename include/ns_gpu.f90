@@ -10,7 +10,8 @@ module ns_gpu
   implicit none
 
   integer(c_int), parameter :: NS_OK = 0, NS_ERR_SHAPE = 1, NS_ERR_CUDA = 2, NS_ERR_NONFINITE = 3, &
-                               NS_ERR_TIMEOUT = 4, NS_ERR_UNSUPPORTED_BC = 5, NS_ERR_ARG = 6, NS_ERR_NOMEM = 7
+                               NS_ERR_TIMEOUT = 4, NS_ERR_UNSUPPORTED_BC = 5, NS_ERR_ARG = 6, NS_ERR_NOMEM = 7, &
+                               NS_ERR_IO = 8
   integer(c_int), parameter :: NS_EULER = 0, NS_AB2 = 1, NS_AB2_CN = 2
 
   type, bind(C) :: ns_config
@@ -225,6 +226,24 @@ module ns_gpu
       real(c_double), intent(in) :: gu(*), gv(*), gw(*)          ! dJ/du(T), dJ/dv(T), dJ/dw(T)
       real(c_double), intent(out) :: du0(*), dv0(*), dw0(*)      ! dJ/du(0) ...
       real(c_double), intent(out), optional :: dhx(*), dhy(*), dhz(*)
+    end function
+
+    ! The session's state as a snapshot in the layout of big_periodic_3D.f90:630-651
+    ! (no libhdf5 needed), and the restart of :309-324 from such a file.
+    integer(c_int) function ns_h5_write_state(h, path, time, time_step, overwrite) bind(C, name="ns_h5_write_state")
+      import :: c_int, c_ptr, c_char, c_double
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: path(*)   ! NUL-terminated
+      real(c_double), value :: time
+      integer(c_int), value :: time_step, overwrite
+    end function
+
+    integer(c_int) function ns_h5_read_state(h, path, time, time_step) bind(C, name="ns_h5_read_state")
+      import :: c_int, c_ptr, c_char, c_double
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: path(*)
+      real(c_double), intent(out), optional :: time
+      integer(c_int), intent(out), optional :: time_step
     end function
   end interface
 end module ns_gpu

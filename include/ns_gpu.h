@@ -39,11 +39,14 @@ enum {
   NS_ERR_SHAPE = 1,          /* unsupported / inconsistent grid size            */
   NS_ERR_CUDA = 2,           /* a CUDA runtime call failed                      */
   NS_ERR_NONFINITE = 3,      /* NaN/Inf found by a checked call                 */
-  NS_ERR_TIMEOUT = 4,        /* a bounded device wait ran out (no kernel of this
-                                build waits on a flag, so none returns it)       */
+  NS_ERR_TIMEOUT = 4,        /* a bounded device wait ran out: the predictor's
+                                tile loader gave up on an mbarrier (ns_get_diag
+                                reports it; the state is then invalid)           */
   NS_ERR_UNSUPPORTED_BC = 5, /* bc/pbc/scheme combination the step cannot run   */
   NS_ERR_ARG = 6,            /* NULL or out-of-range argument                   */
-  NS_ERR_NOMEM = 7           /* device allocation failed                        */
+  NS_ERR_NOMEM = 7,          /* device (or host staging) allocation failed      */
+  NS_ERR_IO = 8              /* a file could not be read or written, or is not
+                                of the HDF5 subset the ns_h5_* calls handle      */
 };
 
 /* Time schemes (big_periodic_3D.f90:350-490). */
@@ -376,6 +379,71 @@ int ns_adj_forward(ns_handle* h, int nsteps, int ckpt_every);
  * and dp_flag = 0. */
 int ns_adj_backward(ns_handle* h, const double* dJ_du, const double* dJ_dv, const double* dJ_dw, double* grad_u,
                     double* grad_v, double* grad_w, double* grad_hx, double* grad_hy, double* grad_hz);
+
+/* ------------------------------------------------------------------------
+ * HDF5 files of the reference, without libhdf5 (host-only; need no GPU)
+ *
+ * The reference's snapshots, restarts and sub-block records go through the
+ * HDF5 Fortran API (big_periodic_3D.f90:593-726).  These calls read and write
+ * the same files: version 0 superblock, version 1 object headers, symbol-table
+ * groups, contiguous little-endian double datasets, and one-value int32 /
+ * double / fixed-string attributes.  Dims are given in Fortran order and data
+ * in Fortran memory order, as in the Fortran API (the file's dataspace holds
+ * the dims reversed).  Raw data is written when a dataset is written; every
+ * ns_h5_flush / ns_h5_close leaves a complete file.  Files outside the subset
+ * (chunked or compressed datasets, the newer object headers) give NS_ERR_IO.
+ * ------------------------------------------------------------------------ */
+typedef struct ns_h5 ns_h5;
+
+/* h5fcreate_f (H5F_ACC_EXCL_F unless overwrite; big_periodic_3D.f90:593,605,630). */
+int ns_h5_create(const char* path, int overwrite, ns_h5** f);
+/* h5fopen_f, H5F_ACC_RDONLY_F (writable = 0; :296, :309) or H5F_ACC_RDWR_F
+ * (writable = 1; :655-662): an existing file's groups, datasets and
+ * attributes are kept, new ones are added. */
+int ns_h5_open(const char* path, int writable, ns_h5** f);
+/* Write the metadata so that the file on disk is complete (the reference closes and
+ * reopens its record files for this, :652-662). */
+int ns_h5_flush(ns_h5* f);
+/* h5fclose_f: flush and close; f is freed whatever the status. */
+int ns_h5_close(ns_h5* f);
+/* Why the last call on f failed; with f = NULL, why the last ns_h5_create,
+ * ns_h5_open or ns_h5_close of this thread failed. */
+const char* ns_h5_last_error(const ns_h5* f);
+
+/* h5gcreate_f (:672, :716): group path "t_1.0000" or "a/b" (the parent must exist). */
+int ns_h5_group(ns_h5* f, const char* path);
+/* h5ltset_attribute_int_f / _double_f with one value, h5ltset_attribute_string_f
+ * (:594-601): on the object at obj ("/" is the root); an attribute of the same
+ * name is replaced. */
+int ns_h5_attr_int(ns_h5* f, const char* obj, const char* name, int value);
+int ns_h5_attr_double(ns_h5* f, const char* obj, const char* name, double value);
+int ns_h5_attr_string(ns_h5* f, const char* obj, const char* name, const char* value);
+/* h5ltmake_dataset_double_f (:644-650, :674-709): a new dataset at path. */
+int ns_h5_write_double(ns_h5* f, const char* path, int rank, const long long* dims, const double* data);
+
+/* h5ltget_dataset_info_f: rank and dims (Fortran order, up to 32). */
+int ns_h5_dims(ns_h5* f, const char* path, int* rank, long long* dims);
+/* h5ltread_dataset_double_f (:298-301, :311-317): the whole dataset into out;
+ * NS_ERR_SHAPE unless its dims are the buffer's dims.  Integer and 4-byte
+ * float datasets are converted. */
+int ns_h5_read_double(ns_h5* f, const char* path, int rank, const long long* dims, double* out);
+/* One attribute value (the first element). */
+int ns_h5_get_attr_int(ns_h5* f, const char* obj, const char* name, long long* value);
+int ns_h5_get_attr_double(ns_h5* f, const char* obj, const char* name, double* value);
+int ns_h5_get_attr_string(ns_h5* f, const char* obj, const char* name, char* buf, int buflen);
+/* The members of a group, sorted, one per line, groups with a trailing '/';
+ * *needed = bytes including the final NUL (buf may be NULL to ask for it). */
+int ns_h5_members(ns_h5* f, const char* group, char* buf, long long buflen, long long* needed);
+
+/* The session's state as a reference snapshot (:630-651): root attributes nx
+ * (ny, nz too for a non-cubic box), dt, nu, time_scheme, time_step, time, and
+ * datasets u, v, w, p, rhs_x_previous, rhs_y_previous, rhs_z_previous. */
+int ns_h5_write_state(ns_handle* h, const char* path, double time, int time_step, int overwrite);
+/* Restart from such a file (:309-324): u, v, w, p and, when the file has
+ * them, the three histories (then the next step is AB2 or AB2-CN; without
+ * them, as in the init file of :296-301, the Euler start).  time and
+ * time_step (may be NULL) receive the root attributes (0 if absent). */
+int ns_h5_read_state(ns_handle* h, const char* path, double* time, int* time_step);
 
 #ifdef __cplusplus
 }

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libns_gpu.so")
 
 NS_OK = 0
 STATUS = {0: "NS_OK", 1: "NS_ERR_SHAPE", 2: "NS_ERR_CUDA", 3: "NS_ERR_NONFINITE", 4: "NS_ERR_TIMEOUT",
-          5: "NS_ERR_UNSUPPORTED_BC", 6: "NS_ERR_ARG", 7: "NS_ERR_NOMEM"}
+          5: "NS_ERR_UNSUPPORTED_BC", 6: "NS_ERR_ARG", 7: "NS_ERR_NOMEM", 8: "NS_ERR_IO"}
 
 
 class NSConfig(C.Structure):
@@ -105,6 +105,25 @@ SIGNATURES = {
     "ns_spectrum": (C.c_int, [C.c_void_p, _DP, _DP, C.POINTER(C.c_longlong), _DP]),
     "ns_adj_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ns_adj_backward": (C.c_int, [C.c_void_p] + [_DP] * 9),
+    # HDF5 files of the reference (host-only)
+    "ns_h5_create": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "ns_h5_open": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "ns_h5_flush": (C.c_int, [C.c_void_p]),
+    "ns_h5_close": (C.c_int, [C.c_void_p]),
+    "ns_h5_last_error": (C.c_char_p, [C.c_void_p]),
+    "ns_h5_group": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "ns_h5_attr_int": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int]),
+    "ns_h5_attr_double": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_double]),
+    "ns_h5_attr_string": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p]),
+    "ns_h5_write_double": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_longlong), _DP]),
+    "ns_h5_dims": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "ns_h5_read_double": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_longlong), _DP]),
+    "ns_h5_get_attr_int": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_longlong)]),
+    "ns_h5_get_attr_double": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, _DP]),
+    "ns_h5_get_attr_string": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int]),
+    "ns_h5_members": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_longlong, C.POINTER(C.c_longlong)]),
+    "ns_h5_write_state": (C.c_int, [C.c_void_p, C.c_char_p, C.c_double, C.c_int, C.c_int]),
+    "ns_h5_read_state": (C.c_int, [C.c_void_p, C.c_char_p, _DP, C.POINTER(C.c_int)]),
 }
 
 _lib = None

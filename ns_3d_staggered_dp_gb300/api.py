@@ -422,3 +422,120 @@ def write_err_csv(path, kind, rows):
     s = lib.ns_write_err_csv(str(path).encode(), int(kind), r.shape[0], _ptr(r))
     if s != 0:
         raise NSError(s, f"cannot write {path}")
+
+
+class H5File:
+    """A file of the reference's HDF5 subset (ns_h5_*; needs no GPU).
+
+    ``H5File(path, "w")`` creates (``"w!"`` overwrites), ``"r"`` opens read-only,
+    ``"a"`` opens for adding groups, datasets and attributes.  Arrays are
+    written and read in their Fortran shapes, as h5ltmake_dataset_double_f and
+    h5ltread_dataset_double_f take them."""
+
+    def __init__(self, path, mode="r"):
+        self.lib = _lib.load()
+        self.h = C.c_void_p()
+        p = str(path).encode()
+        if mode in ("w", "w!"):
+            s = self.lib.ns_h5_create(p, int(mode == "w!"), C.byref(self.h))
+        elif mode in ("r", "a"):
+            s = self.lib.ns_h5_open(p, int(mode == "a"), C.byref(self.h))
+        else:
+            raise NSError(6, f"mode {mode!r}")
+        if s != 0:
+            raise NSError(s, self.lib.ns_h5_last_error(None).decode())
+
+    def _check(self, s):
+        if s != 0:
+            raise NSError(s, self.lib.ns_h5_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            h, self.h = self.h, C.c_void_p()
+            s = self.lib.ns_h5_close(h)
+            if s != 0:
+                raise NSError(s, self.lib.ns_h5_last_error(None).decode())
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def flush(self):
+        self._check(self.lib.ns_h5_flush(self.h))
+
+    def group(self, path):
+        self._check(self.lib.ns_h5_group(self.h, path.encode()))
+
+    def set_attr(self, obj, name, value):
+        """An int, float or str attribute on obj ("/" is the root)."""
+        o, n = obj.encode(), name.encode()
+        if isinstance(value, str):
+            self._check(self.lib.ns_h5_attr_string(self.h, o, n, value.encode()))
+        elif isinstance(value, (int, np.integer)) and not isinstance(value, bool):
+            self._check(self.lib.ns_h5_attr_int(self.h, o, n, int(value)))
+        else:
+            self._check(self.lib.ns_h5_attr_double(self.h, o, n, float(value)))
+
+    def attr(self, obj, name, kind=float):
+        o, n = obj.encode(), name.encode()
+        if kind is str:
+            buf = C.create_string_buffer(4096)
+            self._check(self.lib.ns_h5_get_attr_string(self.h, o, n, buf, len(buf)))
+            return buf.value.decode()
+        if kind is int:
+            v = C.c_longlong()
+            self._check(self.lib.ns_h5_get_attr_int(self.h, o, n, C.byref(v)))
+            return v.value
+        v = C.c_double()
+        self._check(self.lib.ns_h5_get_attr_double(self.h, o, n, C.byref(v)))
+        return v.value
+
+    def write(self, path, a):
+        a = np.asfortranarray(a, dtype=np.float64)
+        dims = (C.c_longlong * a.ndim)(*a.shape)
+        self._check(self.lib.ns_h5_write_double(self.h, path.encode(), a.ndim, dims, _ptr(a)))
+
+    def shape(self, path):
+        r = C.c_int()
+        d = (C.c_longlong * 32)()
+        self._check(self.lib.ns_h5_dims(self.h, path.encode(), C.byref(r), d))
+        return tuple(d[i] for i in range(r.value))
+
+    def read(self, path, shape=None):
+        shape = tuple(shape) if shape is not None else self.shape(path)
+        out = np.zeros(shape, order="F")
+        dims = (C.c_longlong * max(1, len(shape)))(*shape)
+        self._check(self.lib.ns_h5_read_double(self.h, path.encode(), len(shape), dims, _ptr(out)))
+        return out
+
+    def members(self, group="/"):
+        need = C.c_longlong()
+        self._check(self.lib.ns_h5_members(self.h, group.encode(), None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        self._check(self.lib.ns_h5_members(self.h, group.encode(), buf, need.value, None))
+        return [x for x in buf.value.decode().split("\n") if x]
+
+
+def _session_h5_write_state(self, path, time=0.0, time_step=0, overwrite=False):
+    """The state as a reference snapshot (big_periodic_3D.f90:630-651)."""
+    self._check(self.lib.ns_h5_write_state(self.h, str(path).encode(), float(time), int(time_step), int(overwrite)))
+
+
+def _session_h5_read_state(self, path):
+    """Restart from a snapshot (big_periodic_3D.f90:309-324); returns (time, time_step)."""
+    t = C.c_double()
+    ts = C.c_int()
+    self._check(self.lib.ns_h5_read_state(self.h, str(path).encode(), C.byref(t), C.byref(ts)))
+    return t.value, ts.value
+
+
+Session.h5_write_state = _session_h5_write_state
+Session.h5_read_state = _session_h5_read_state

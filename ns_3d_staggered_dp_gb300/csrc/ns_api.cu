@@ -1006,6 +1006,7 @@ const char* ns_status_string(int s) {
     case NS_ERR_UNSUPPORTED_BC: return "unsupported boundary condition";
     case NS_ERR_ARG: return "bad argument";
     case NS_ERR_NOMEM: return "out of device memory";
+    case NS_ERR_IO: return "file read/write failed or the file is outside the HDF5 subset";
     default: return "unknown status";
   }
 }
