@@ -1060,10 +1060,11 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
   if (cudaMalloc(&h->diag_bits, sizeof(unsigned long long)) != cudaSuccess) return bail(NS_ERR_NOMEM);
   if (cudaMalloc(&h->dev_err, sizeof(int)) != cudaSuccess) return bail(NS_ERR_NOMEM);
   if (cudaMemsetAsync(h->dev_err, 0, sizeof(int), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
-  // without the driver's map encoder (or with NS_PREDICT_TMA=0 in the environment)
-  // the predictor stages its tiles with cp.async; the results are the same bits
+  // The predictor stages its tiles with cp.async.  NS_PREDICT_TMA=1 in the
+  // environment selects the tensor-memory-access loader instead (the same
+  // bits; measured 3.3 ms against 2.1 ms per 256^3 launch, so not the default).
   const char* tma_env = std::getenv("NS_PREDICT_TMA");
-  if (!(tma_env && tma_env[0] == '0')) ns::make_pred_tma(h->tma, h->L, h->u, h->v, h->w);
+  if (tma_env && tma_env[0] == '1') ns::make_pred_tma(h->tma, h->L, h->u, h->v, h->w);
   if ((s = build_plans(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
   if ((s = build_adi(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);

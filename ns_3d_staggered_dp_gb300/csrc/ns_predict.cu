@@ -89,6 +89,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Wait for the phase `parity` of a slot; false once kWaitLimit polls or
 // kWaitNs found it incomplete (the caller records the error).
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  // the common case (the plane has landed) reads no timer: a %globaltimer
+  // read is a long-latency special-register access on every plane's path
+  if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (int it = 0; it < kWaitLimit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;

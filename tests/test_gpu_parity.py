@@ -266,9 +266,9 @@ def test_nonfinite_state_is_reported():
     ((64, 32, 32), {"bc": (1, 1, 2), "pbc": (1, 1, 3), "dp_flag": 1}),
 ])
 def test_predictor_tile_loaders_agree(case, monkeypatch):
-    """The predictor stages its tiles with the tensor-memory-access loader
-    (cp.async.bulk.tensor into an mbarrier ring) unless NS_PREDICT_TMA=0 at
-    ns_create selects the cp.async loader: both give the same bits, for the
+    """The predictor stages its tiles with cp.async, or with the
+    tensor-memory-access loader (cp.async.bulk.tensor into an mbarrier ring)
+    when NS_PREDICT_TMA=1 at ns_create: both give the same bits, for the
     device-resident step and for ns_step_host, on full and ragged tiles."""
     n, kw = case
     kw = dict(kw)
