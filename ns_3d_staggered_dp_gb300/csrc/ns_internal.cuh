@@ -43,7 +43,9 @@ inline Layout make_layout(int nx, int ny, int nz) {
   L.px = ((nx + 2 + 7 + 7) / 8) * 8;
   L.sy = L.px;
   L.sz = (long long)L.px * (ny + 2);
-  L.fsize = L.sz * (nz + 2) + 8;
+  // the predictor's 16-byte tile copies read whole rows from slot -1 to
+  // slot 32 bx + 33, up to 25 doubles past the last row of the last plane
+  L.fsize = L.sz * (nz + 2) + 32;
   return L;
 }
 
@@ -64,6 +66,11 @@ __device__ __forceinline__ double fmul(const FOne& c, double a, double b) { retu
 __device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+// 16-byte copies (both addresses 16-byte aligned; through L2 only).
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>

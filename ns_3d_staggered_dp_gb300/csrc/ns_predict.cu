@@ -35,9 +35,8 @@ namespace {
 constexpr int TX = 32;
 constexpr int TY = 16;
 constexpr int KC = 16;
-constexpr int SXL = TX + 2;  // x positions loaded: [i0-1, i0+32]
-constexpr int SXW = TX + 8;  // smem row width: column c is x = i0-2+c (a 320-byte row, the
-                             // tile loader's box; slot i0-1 is column 1)
+constexpr int SXW = TX + 8;  // smem row width: column c is x = i0-2+c; columns 1..34 (x in
+                             // [i0-1, i0+32]) are read, 0..35 loaded (a 320-byte row)
 constexpr int SYH = TY + 2;  // smem rows: y in [j0-1, j0+TY]
 constexpr int PXW = TX + 1;  // product row width: x in [i0-1, i0+31]
 constexpr int PYH = TY + 1;  // product rows: y in [j0-1, j0+TY-1]
@@ -122,21 +121,26 @@ __device__ __forceinline__ void tma_plane(PredSmem& S, const CUtensorMap* mu, co
 
 
 // Start copying plane k (clamped into the box) of u, v, w into ring slot s
-// (cp.async; the caller commits the group).
+// (cp.async; the caller commits the group).  Each smem row is 18 16-byte
+// copies of slots i0-2 .. i0+33: index 7 + i0 - 2 = 32 bx + 6 (plus whole
+// rows and planes of 8-double multiples) keeps every source 16-byte aligned.
+// Rows and planes are clamped into the box; past x = nx + 1 the copies read
+// row padding (or the next row, or the field's tail padding), which only
+// positions without an output use.
 __device__ __forceinline__ void issue_plane(PredSmem& S, const Layout& L, const double* __restrict__ u,
                                             const double* __restrict__ v, const double* __restrict__ w, int i0,
                                             int j0, int k, int s) {
+  constexpr int NV = (TX + 4) / 2;
   const int kk = clampi(k, 0, L.nz + 1);
   const int nthr = blockDim.x * blockDim.y;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y;
-  for (int e = tid; e < SXL * SYH; e += nthr) {
-    const int xx = e % SXL, yy = e / SXL;
-    const int gi = clampi(i0 - 1 + xx, 0, L.nx + 1);
+  for (int e = tid; e < NV * SYH; e += nthr) {
+    const int xv = e % NV, yy = e / NV;
     const int gj = clampi(j0 - 1 + yy, 0, L.ny + 1);
-    const long long g = L.at(gi, gj, kk);
-    cp_async8(&S.u[s][yy][xx + 1], u + g);
-    cp_async8(&S.v[s][yy][xx + 1], v + g);
-    cp_async8(&S.w[s][yy][xx + 1], w + g);
+    const long long g = L.at(i0 - 2 + 2 * xv, gj, kk);
+    cp_async16(&S.u[s][yy][2 * xv], u + g);
+    cp_async16(&S.v[s][yy][2 * xv], v + g);
+    cp_async16(&S.w[s][yy][2 * xv], w + g);
   }
 }
 
