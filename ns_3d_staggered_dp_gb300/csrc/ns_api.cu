@@ -1168,8 +1168,8 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   // two planes above it that the predictor reads), so compute starts early;
   // then 4 chunks a slab (2-chunk slabs left each launch under one wave of
   // CTAs); the compute of the last slab is not hidden, so the slabs shrink
-  // towards the top: half the rest (whole chunks) once less than two full
-  // slabs remain.
+  // towards the top: half the rest (whole chunks, rounded down) once less
+  // than two full slabs remain (18, 64, 64, 48, 32, 16, 16 planes at 256).
   const int KC = predict_chunk_planes();
   const int S = 4 * KC;
   std::vector<int> fb = {0, std::min(nz + 2, KC + 2)};
@@ -1177,7 +1177,7 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
     const int r = nz + 2 - fb.back();
     int take = r;
     if (r >= 2 * S) take = S;
-    else if (r > KC + 2) take = std::max(KC, (r / 2 + KC - 1) / KC * KC);
+    else if (r > KC + 2) take = std::max(KC, r / 2 / KC * KC);
     fb.push_back(fb.back() + take);
   }
   const int nslab = (int)fb.size() - 1;
