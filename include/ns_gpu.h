@@ -175,6 +175,16 @@ int ns_poisson(ns_handle* h, const double* rhs, double* dp);
 /* The three AB2-CN ADI sweeps on u*, v*, w* in place, with the set-1..3 faces
  * (big_periodic_3D.f90:425-489; re_simulation_sub_tstep_interBC_combine.f90:656-701). */
 int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star);
+/* vel_bc_staggered (NS_functions.f90:213-310) on host u*, v*, w* in place:
+ * the ghost and face values of the session's bc codes and its face set 0
+ * (ns_set_faces).  The session's state is untouched. */
+int ns_vel_bc(ns_handle* h, double* u_star, double* v_star, double* w_star);
+/* Gauge and correction (big_periodic_3D.f90:562-567): with cfg.gauge,
+ * dp -= dp(1,1,1); then u = u* - dt diff(dp)/dx (likewise v, w over the full
+ * padded arrays) and p = dp_flag p + dp.  dp and p are p-shaped; p is read
+ * (with dp_flag = 1) and written.  The session's state is untouched. */
+int ns_correct(ns_handle* h, const double* u_star, const double* v_star, const double* w_star, const double* dp,
+               double* u, double* v, double* w, double* p);
 
 /* The periodic FFT pressure Poisson solve of ns_poisson without any device
  * allocation.  No counterpart in the reference: it serves callers that must

@@ -105,6 +105,8 @@ SIGNATURES = {
     "ns_spectrum": (C.c_int, [C.c_void_p, _DP, _DP, C.POINTER(C.c_longlong), _DP]),
     "ns_adj_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "ns_adj_backward": (C.c_int, [C.c_void_p] + [_DP] * 9),
+    "ns_vel_bc": (C.c_int, [C.c_void_p, _DP, _DP, _DP]),
+    "ns_correct": (C.c_int, [C.c_void_p] + [_DP] * 8),
     # HDF5 files of the reference (host-only)
     "ns_h5_create": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
     "ns_h5_open": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),

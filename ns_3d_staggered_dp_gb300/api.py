@@ -212,6 +212,24 @@ class Session:
         self._check(self.lib.ns_adi(self.h, _ptr(us), _ptr(vs), _ptr(ws)))
         return us, vs, ws
 
+    def vel_bc(self, us, vs, ws):
+        """vel_bc_staggered on u*, v*, w* with the session's bc and face set 0 (returns new arrays)."""
+        sh = self.shapes
+        us, vs, ws = (np.array(_f(us, sh["u"]), order="F"), np.array(_f(vs, sh["v"]), order="F"),
+                      np.array(_f(ws, sh["w"]), order="F"))
+        self._check(self.lib.ns_vel_bc(self.h, _ptr(us), _ptr(vs), _ptr(ws)))
+        return us, vs, ws
+
+    def correct(self, us, vs, ws, dp, p):
+        """Gauge and correction (big_periodic_3D.f90:562-567): returns u, v, w, p."""
+        sh = self.shapes
+        ins = [_f(us, sh["u"]), _f(vs, sh["v"]), _f(ws, sh["w"]), _f(dp, sh["p"])]
+        out = {k: np.zeros(sh[k], order="F") for k in ("u", "v", "w")}
+        out["p"] = np.array(_f(p, sh["p"]), order="F")
+        self._check(self.lib.ns_correct(self.h, *[_ptr(a) for a in ins], _ptr(out["u"]), _ptr(out["v"]),
+                                        _ptr(out["w"]), _ptr(out["p"])))
+        return out
+
     def error_metrics(self, u_ref, v_ref, w_ref, p_ref):
         """rms_vel(1..4) + err_vel(1..8) of the current state against reference
         arrays (ns_error_metrics, re_simulation_sub_tstep_interBC_combine.f90:813-834)."""

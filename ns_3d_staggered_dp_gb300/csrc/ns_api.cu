@@ -1593,4 +1593,46 @@ int ns_adi(ns_handle* h, double* u_star, double* v_star, double* w_star) {
   return NS_OK;
 }
 
+int ns_vel_bc(ns_handle* h, double* u_star, double* v_star, double* w_star) {
+  if (!h || !u_star || !v_star || !w_star) return NS_ERR_ARG;
+  const ns_config& c = h->cfg;
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  NS_CUDA(h, h2d_field(h, h->us, u_star, 0));
+  NS_CUDA(h, h2d_field(h, h->vs, v_star, 1));
+  NS_CUDA(h, h2d_field(h, h->ws, w_star, 2));
+  NS_CUDA(h, launch_vel_bc(h->L, h->us, h->vs, h->ws, h->faces[0], c.bc, h->stream));
+  NS_CUDA(h, d2h_field(h, u_star, h->us, 0));
+  NS_CUDA(h, d2h_field(h, v_star, h->vs, 1));
+  NS_CUDA(h, d2h_field(h, w_star, h->ws, 2));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
+int ns_correct(ns_handle* h, const double* u_star, const double* v_star, const double* w_star, const double* dp,
+               double* u, double* v, double* w, double* p) {
+  if (!h || !u_star || !v_star || !w_star || !dp || !u || !v || !w || !p) return NS_ERR_ARG;
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  struct DevBuf {
+    double* ptr = nullptr;
+    ~DevBuf() { if (ptr) cudaFree(ptr); }
+  } pt;
+  NS_CUDA(h, cudaMalloc(&pt.ptr, h->L.fsize * sizeof(double)));
+  NS_CUDA(h, cudaMemsetAsync(pt.ptr, 0, h->L.fsize * sizeof(double), h->stream));
+  NS_CUDA(h, h2d_field(h, h->us, u_star, 0));
+  NS_CUDA(h, h2d_field(h, h->vs, v_star, 1));
+  NS_CUDA(h, h2d_field(h, h->ws, w_star, 2));
+  NS_CUDA(h, h2d_field(h, h->dp, dp, 3));
+  NS_CUDA(h, h2d_field(h, pt.ptr, p, 3));
+  CorrectArgs ca = correct_args(h);
+  ca.us = h->us; ca.vs = h->vs; ca.ws = h->ws; ca.dp = h->dp;
+  ca.u = h->us2; ca.v = h->vs2; ca.w = h->ws2; ca.p = pt.ptr;
+  NS_CUDA(h, launch_correct(ca, h->stream));
+  NS_CUDA(h, d2h_field(h, u, h->us2, 0));
+  NS_CUDA(h, d2h_field(h, v, h->vs2, 1));
+  NS_CUDA(h, d2h_field(h, w, h->ws2, 2));
+  NS_CUDA(h, d2h_field(h, p, pt.ptr, 3));
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
 }  // extern "C"

@@ -985,6 +985,16 @@ def _ranges(cfg):
     return r0, r1
 
 
+def correct(us, vs, ws, dp, p, dx, dy, dz, dt, dp_flag, gauge=1):
+    """Gauge and correction, big_periodic_3D.f90:562-567: dp -= dp(1,1,1);
+    u = -dt diff(dp,1,1)/dx + u_star (v, w likewise); p = dp_flag p + dp.
+    Returns (u, v, w, p); the inputs are not modified."""
+    if gauge:
+        dp = dp - dp[0, 0, 0]
+    return (-dt * diff(dp, 1, 1) / dx + us, -dt * diff(dp, 1, 2) / dy + vs, -dt * diff(dp, 1, 3) / dz + ws,
+            dp_flag * p + dp)
+
+
 def poisson_solve(R, cfg, faces, solver="auto"):
     """Interior dp from the (BC-modified) RHS for any pbc mix."""
     dx, dy, dz = cfg.h
@@ -1072,12 +1082,7 @@ def step(st, cfg, faces=None, cn_faces=None, cnf=None, solver="auto", return_par
     dp = np.zeros((nx + 2, ny + 2, nz + 2))
     dp[1:-1, 1:-1, 1:-1] = poisson_solve(R, cfg, faces, solver)
     pr_bc_staggered(dp, faces, cfg.pbc, dx, dy, dz)
-    if cfg.gauge:
-        dp = dp - dp[0, 0, 0]
-    un = -dt * diff(dp, 1, 1) / dx + us
-    vn = -dt * diff(dp, 1, 2) / dy + vs
-    wn = -dt * diff(dp, 1, 3) / dz + ws
-    pn = dpf * p + dp
+    un, vn, wn, pn = correct(us, vs, ws, dp, p, dx, dy, dz, dt, dpf, cfg.gauge)
     # history outside the interior ranges is never read; keep it zero
     hx = np.zeros_like(px); hy = np.zeros_like(py); hz = np.zeros_like(pz)
     hx[X] = px[X]; hy[Y] = py[Y]; hz[Z] = pz[Z]

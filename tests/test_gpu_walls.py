@@ -195,3 +195,48 @@ def test_unsupported_mixes_rejected():
         cfg = O.Config(kw["nx"], kw["ny"], kw["nz"], bc=kw["bc"], pbc=kw["pbc"])
         with pytest.raises(NSError):
             session(cfg)
+
+
+ROUTINE_BCS = [(1, 1, 1), (1, 2, 1), (1, 1, 2), (1, 2, 2), (2, 2, 2)]  # a wall x needs walls in y and z
+
+
+@pytest.mark.parametrize("bc", ROUTINE_BCS)
+def test_vel_bc_routine(bc):
+    """ns_vel_bc against vel_bc_staggered (NS_functions.f90:213-310) with
+    random face values: periodic images and wall ghosts/faces."""
+    pbc = tuple(1 if b == 1 else 3 for b in bc)
+    cfg = O.Config(32, 16, 32, lx=1.0, ly=0.7, lz=1.2, bc=bc, pbc=pbc)
+    st = random_state(cfg, 29)
+    rng = np.random.default_rng(31)
+    us, vs, ws = (rng.standard_normal(a.shape) for a in (st.u, st.v, st.w))
+    faces = random_faces(cfg, 37)
+    ref = [us.copy(), vs.copy(), ws.copy()]
+    O.vel_bc_staggered(*ref, faces, *bc)
+    with session(cfg) as s:
+        s.set_faces(faces.d, 0)
+        got = s.vel_bc(us, vs, ws)
+    for a, b in zip(got, ref):
+        assert a.shape == b.shape
+        assert np.max(np.abs(a - b)) <= 1e-13 * max(1.0, np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("bc", [(1, 1, 1), (1, 2, 1), (2, 2, 2)])
+@pytest.mark.parametrize("dp_flag,gauge", [(0, 1), (1, 1), (1, 0)])
+def test_correct_routine(bc, dp_flag, gauge):
+    """ns_correct against the gauge and correction of
+    big_periodic_3D.f90:562-567 over the full padded arrays."""
+    pbc = tuple(1 if b == 1 else 3 for b in bc)
+    cfg = O.Config(32, 16, 32, lx=1.0, ly=0.7, lz=1.2, dt=0.003, bc=bc, pbc=pbc, dp_flag=dp_flag, gauge=gauge)
+    st = random_state(cfg, 41)
+    rng = np.random.default_rng(43)
+    us, vs, ws = (rng.standard_normal(a.shape) for a in (st.u, st.v, st.w))
+    dp = rng.standard_normal(st.p.shape)
+    p = rng.standard_normal(st.p.shape)
+    dx, dy, dz = cfg.h
+    ref = O.correct(us, vs, ws, dp, p, dx, dy, dz, cfg.dt, dp_flag, gauge)
+    with session(cfg) as s:
+        got = s.correct(us, vs, ws, dp, p)
+    for k, b in zip(("u", "v", "w", "p"), ref):
+        a = got[k]
+        assert a.shape == b.shape, k
+        assert np.max(np.abs(a - b)) <= 1e-13 * max(1.0, np.max(np.abs(b))), k
