@@ -132,6 +132,22 @@ module ns_gpu
       real(c_double), intent(inout) :: us(*), vs(*), ws(*)
     end function
 
+    ! vel_bc_staggered (NS_functions.f90:213-310) with the session's bc and face set 0
+    integer(c_int) function ns_vel_bc(h, us, vs, ws) bind(C, name="ns_vel_bc")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(inout) :: us(*), vs(*), ws(*)
+    end function
+
+    ! gauge + correction (big_periodic_3D.f90:562-567): u = u_star - dt0*diff(dp,1,1)/dx ..., p = dp_flag*p + dp
+    integer(c_int) function ns_correct(h, us, vs, ws, dp, u, v, w, p) bind(C, name="ns_correct")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: us(*), vs(*), ws(*), dp(*)
+      real(c_double), intent(out) :: u(*), v(*), w(*)
+      real(c_double), intent(inout) :: p(*)
+    end function
+
     ! --- batched re-simulation --------------------------------------------------
     subroutine ns_batch_config_default(cfg) bind(C, name="ns_batch_config_default")
       import :: ns_batch_config
