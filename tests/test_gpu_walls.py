@@ -240,3 +240,30 @@ def test_correct_routine(bc, dp_flag, gauge):
         a = got[k]
         assert a.shape == b.shape, k
         assert np.max(np.abs(a - b)) <= 1e-13 * max(1.0, np.max(np.abs(b))), k
+
+
+def test_nan_poisoned_faces_are_reported():
+    """A NaN in one boundary face array (the parent data of a re-simulation)
+    reaches the interior: a pressure face of set 0 enters the Poisson
+    right-hand side and the pressure ghosts (with AB2-CN the velocity faces
+    of set 0 are not read: the sweeps take sets 1-3).  ns_get_diag reports
+    it as NS_ERR_NONFINITE, and the handle runs a clean step once the faces
+    are replaced."""
+    from ns_3d_staggered_dp_gb300 import NSError
+    cfg = O.Config(32, 16, 32, lx=1.0, ly=0.7, lz=1.2, nu=0.02, dt=0.002, bc=(1, 2, 1), pbc=(1, 3, 1),
+                   scheme=O.AB2_CN)
+    st = random_state(cfg, 47)
+    good = random_faces(cfg, 53, amp=0.1)
+    bad = {k: v.copy() for k, v in good.d.items()}
+    bad["y_p_1"][7, 9] = np.nan
+    with session(cfg) as s:
+        s.set_faces(bad, 0)
+        s.set_state(st.u, st.v, st.w, st.p)
+        s.step(1)
+        with pytest.raises(NSError) as e:
+            s.diag()
+        assert e.value.status == 3
+        s.set_faces(good.d, 0)
+        s.set_state(st.u, st.v, st.w, st.p)
+        s.step(1)
+        assert np.isfinite(s.diag()["max_div"])
