@@ -7,8 +7,8 @@ sub_tstep sub-steps in the first interval with the AB2 history saved and
 restored (:443-454, :602-612), the DCT pressure solve with the mean of the
 parent's dp (:766-768).
 
-Tolerances: 1e-10 relative L2 per field against the oracle (the north-star
-bound); the exact-replay property P1 of the reference's err_file
+Tolerances: 1e-10 relative L2 per field against the oracle (the parity
+bound of the step); the exact-replay property P1 of the reference's err_file
 (err_vel_AB2_4.E-3_N_Ustar_TOffset_restart.txt: 4.5e-15 over the run) is
 checked at 1e-11 relative L2 against the GPU parent's own sub-blocks;
 batched and per-subdomain-loop launches must agree bit for bit.

@@ -3,7 +3,7 @@
 Tolerances: the step is FP64 with the same algebra as the reference but
 different rounding (FMA folding, MKL vs our FFT/Thomas); routine-level
 results must agree to a relative L2 of 1e-12, ten full steps to 1e-10 per
-field (the benchmark spec's bound), and max|div u| <= 1e-12 after every step.
+field (the parity bound of the step), and max|div u| <= 1e-12 after every step.
 """
 import numpy as np
 import pytest
