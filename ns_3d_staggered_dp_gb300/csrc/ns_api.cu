@@ -1063,8 +1063,14 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
   // The predictor stages its tiles with cp.async.  NS_PREDICT_TMA=1 in the
   // environment selects the tensor-memory-access loader instead (the same
   // bits; measured 3.3 ms against 2.1 ms per 256^3 launch, so not the default).
+  // A requested loader that cannot be set up fails ns_create rather than
+  // running the other one silently.
   const char* tma_env = std::getenv("NS_PREDICT_TMA");
-  if (tma_env && tma_env[0] == '1') ns::make_pred_tma(h->tma, h->L, h->u, h->v, h->w);
+  if (tma_env && tma_env[0] == '1' && !ns::make_pred_tma(h->tma, h->L, h->u, h->v, h->w)) {
+    h->err = "NS_PREDICT_TMA=1: the tile loader's tensor maps could not be encoded";
+    std::fprintf(stderr, "ns_create: %s\n", h->err.c_str());
+    return bail(NS_ERR_CUDA);
+  }
   if ((s = build_plans(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
   if ((s = build_adi(h)) != NS_OK) { std::fprintf(stderr, "ns_create: %s\n", h->err.c_str()); return bail(s); }
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
