@@ -709,10 +709,21 @@ int step_host_slab_tail(ns_handle* h, const std::vector<int>& tb, double* uo, do
   const int nz = c.nz;
   const DivArgs d = div_args(h, nullptr);
   NS_CUDA(h, launch_poisson_fwd(h->plan, d, h->spec, h->dp, L, h->stream, marker(h)));
+  // A middle inverse pass that needs whole z lines (the z FFT of a y-wall
+  // box, or a dense y transform) runs on the whole box first; the x inverse
+  // pass, the ghost fill and the correction then go slab by slab.
+  const bool mid_planes = poisson_inv_by_planes(h->plan);
+  if (!mid_planes) NS_CUDA(h, launch_poisson_inv_mid(h->plan, d, h->spec, L, h->stream, marker(h), 1, nz + 1));
   trace_mark(h, h->stream, "poisson fwd");
+  auto inv = [&](int k0, int k1) -> cudaError_t {
+    cudaError_t e = mid_planes ? launch_poisson_inv_mid(h->plan, d, h->spec, L, h->stream, marker(h), k0, k1)
+                               : cudaSuccess;
+    if (e == cudaSuccess) e = launch_poisson_inv_x(h->plan, d, h->spec, h->dp, L, h->stream, marker(h), k0, k1);
+    return e;
+  };
   const CorrectArgs ca = correct_args(h);
   const int top = std::max(1, nz - 1);
-  NS_CUDA(h, launch_poisson_inv(h->plan, d, h->spec, h->dp, L, h->stream, marker(h), top, nz + 1));
+  NS_CUDA(h, inv(top, nz + 1));
   NS_CUDA(h, launch_pr_bc_planes(L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, top, nz + 1, h->stream));
   mark(h, "pr_bc", 2);
   double* want[4] = {uo, vo, wo, po};
@@ -722,7 +733,7 @@ int step_host_slab_tail(ns_handle* h, const std::vector<int>& tb, double* uo, do
     const int lo = tb[s], hi = tb[s + 1];
     const int k0 = std::max(lo, 1), k1 = std::min(hi, top);
     if (k1 > k0) {
-      NS_CUDA(h, launch_poisson_inv(h->plan, d, h->spec, h->dp, L, h->stream, marker(h), k0, k1));
+      NS_CUDA(h, inv(k0, k1));
       NS_CUDA(h, launch_pr_bc_planes(L, h->dp, h->faces[0], c.pbc, h->dx, h->dy, k0, k1, h->stream));
       mark(h, "pr_bc", 2);
     }
@@ -1190,7 +1201,7 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
   // The tail in z-slabs as well when the inverse passes work plane by plane:
   // each slab's u, v, w, p leave while the next slab is computed.  The first
   // slab is small (its compute comes before any of the tail's copies).
-  const bool slab_tail = poisson_inv_by_planes(h->plan);
+  const bool slab_tail = poisson_inv_x_by_planes(h->plan);
   std::vector<int> tb = {0};
   if (slab_tail) {
     // sizes doubling from KC/2 + 1 up to S: each slab's compute about as

@@ -659,18 +659,19 @@ cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec
 }
 
 bool poisson_inv_by_planes(const FftPlan& P) { return P.kind[0] == 0 && P.kind[1] == 0; }
+bool poisson_inv_x_by_planes(const FftPlan& P) { return P.kind[0] == 0; }
 
-// The inverse passes into dp.  With poisson_inv_by_planes(P) both passes
-// work plane by plane in z, and [k0, k1) (cell slots 1..nz) selects planes;
-// otherwise the range must be all of [1, nz + 1).
-cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
-                               cudaStream_t st, const Marker& mk, int k0, int k1) {
+// The inverse pass of the middle axis (y, or z when y is the wall axis of a
+// z-periodic box).  With poisson_inv_by_planes(P) it works plane by plane
+// in z and [k0, k1) (cell slots 1..nz) selects planes; otherwise the range
+// must be all of [1, nz + 1).
+cudaError_t launch_poisson_inv_mid(const FftPlan& P, const DivArgs& d, double2* spec, const Layout& L,
+                                   cudaStream_t st, const Marker& mk, int k0, int k1) {
   const FOne c{d.one, d.mzero};
   cudaError_t e = cudaSuccess;
   if (k0 < 1 || k1 > L.nz + 1 || k0 > k1) return cudaErrorInvalidValue;
   if (k0 == k1) return cudaSuccess;
-  const bool part = k0 != 1 || k1 != L.nz + 1;
-  if (part && !poisson_inv_by_planes(P)) return cudaErrorInvalidValue;
+  if ((k0 != 1 || k1 != L.nz + 1) && !poisson_inv_by_planes(P)) return cudaErrorInvalidValue;
   const int m = P.kind[1] == 2 ? 2 : 1;
   const int nm = m == 1 ? P.ny : P.nz;
   if (P.kind[m] == 0) {
@@ -689,6 +690,18 @@ cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec
     if ((e = launch_dense_yz(m, false, P, spec, st)) != cudaSuccess) return e;
     mk(m == 1 ? "dense_y_inv" : "dense_z_inv");
   }
+  return e;
+}
+
+// The x inverse pass into dp.  With poisson_inv_x_by_planes(P) (an x FFT)
+// it works plane by plane in z; the dense x transform takes the whole box.
+cudaError_t launch_poisson_inv_x(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                                 cudaStream_t st, const Marker& mk, int k0, int k1) {
+  const FOne c{d.one, d.mzero};
+  cudaError_t e = cudaSuccess;
+  if (k0 < 1 || k1 > L.nz + 1 || k0 > k1) return cudaErrorInvalidValue;
+  if (k0 == k1) return cudaSuccess;
+  if ((k0 != 1 || k1 != L.nz + 1) && !poisson_inv_x_by_planes(P)) return cudaErrorInvalidValue;
   if (P.kind[0] == 0) {
 #define X_INV(n) e = launch_x_inv<(n) / 2>(P, spec, dp, L, c, st, k0, k1)
     NS_SIZE_SWITCH(P.nx, X_INV)
@@ -700,6 +713,15 @@ cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec
     mk("dense_x_inv");
   }
   return e;
+}
+
+// Both inverse passes into dp for the cell slots [k0, k1) (see the two
+// functions above for which ranges each plan takes).
+cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                               cudaStream_t st, const Marker& mk, int k0, int k1) {
+  cudaError_t e = launch_poisson_inv_mid(P, d, spec, L, st, mk, k0, k1);
+  if (e != cudaSuccess) return e;
+  return launch_poisson_inv_x(P, d, spec, dp, L, st, mk, k0, k1);
 }
 
 cudaError_t launch_fft_poisson(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,

@@ -275,7 +275,12 @@ cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec
                                cudaStream_t st, const Marker& mk);
 // True when both inverse passes are FFTs along x and y, which work plane by
 // plane in z: launch_poisson_inv then accepts any cell-plane range [k0, k1).
-bool poisson_inv_by_planes(const FftPlan& P);
+bool poisson_inv_by_planes(const FftPlan& P);    // both inverse passes take z plane ranges
+bool poisson_inv_x_by_planes(const FftPlan& P);  // the x inverse pass takes z plane ranges
+cudaError_t launch_poisson_inv_mid(const FftPlan& P, const DivArgs& d, double2* spec, const Layout& L,
+                                   cudaStream_t st, const Marker& mk, int k0, int k1);
+cudaError_t launch_poisson_inv_x(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
+                                 cudaStream_t st, const Marker& mk, int k0, int k1);
 cudaError_t launch_poisson_inv(const FftPlan& P, const DivArgs& d, double2* spec, double* dp, const Layout& L,
                                cudaStream_t st, const Marker& mk, int k0, int k1);
 // Symmetry bits of a dense transform pair of even size n (sym in FftPlan),
