@@ -289,24 +289,32 @@ def oracle_setup(name, n):
     return O, cfg, st, cnf, nx * ny * nz
 
 
-def cpu_stepper(name, n):
+def cpu_stepper(name, n, nthreads=None):
     """(advance_one_step, ncell, description, threads) of the timed CPU baseline:
     the C++/OpenMP restatement of the reference step (oracle/ns_ref_cpu.cpp,
     the reference's own algorithm: dense mat_CN LU solves for the ADI, FFT
     Poisson) on every host thread for the periodic workload; the NumPy/SciPy
-    restatement otherwise (or if the C++ library cannot be built)."""
+    restatement otherwise (or if the C++ library cannot be built).  nthreads
+    (C++ restatement only) limits the OpenMP threads of the steps; the
+    returned restore() puts the process-wide setting back."""
     O, cfg, st, cnf, ncell = oracle_setup(name, n)
     if name == "hit":
         try:
             from oracle.ns_ref_cpu import CpuStep
             cpu = CpuStep(cfg)
             holder = {"st": st}
+            before = cpu.threads()
+            if nthreads:
+                cpu.set_threads(nthreads)
 
             def adv():
                 cpu.step(holder["st"])
 
+            def restore():
+                cpu.set_threads(before)
+
             return adv, ncell, ("C++/OpenMP restatement of the reference step (dense mat_CN LU line solves "
-                                "as getrs, r2c FFT Poisson)"), cpu.threads()
+                                "as getrs, r2c FFT Poisson)"), cpu.threads(), restore
         except Exception:
             pass
     holder = {"st": st}
@@ -314,18 +322,22 @@ def cpu_stepper(name, n):
     def adv_np():
         holder["st"] = O.step(holder["st"], cfg, cnf=cnf)
 
-    return adv_np, ncell, "NumPy/SciPy restatement of the reference step (threaded BLAS)", os.cpu_count()
+    return (adv_np, ncell, "NumPy/SciPy restatement of the reference step (threaded BLAS)", os.cpu_count(),
+            lambda: None)
 
 
-def cpu_baseline_sample(name, n, steps):
-    """The CPU restatement on the host cores, on `steps` steps of the workload
-    at grid size n after one untimed Euler-start step."""
-    adv, ncell, desc, threads = cpu_stepper(name, n)
-    adv()  # warm (Euler start)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        adv()
-    sec = time.perf_counter() - t0
+def cpu_baseline_sample(name, n, steps, nthreads=None):
+    """The CPU restatement on the host cores (or nthreads of them), on `steps`
+    steps of the workload at grid size n after one untimed Euler-start step."""
+    adv, ncell, desc, threads, restore = cpu_stepper(name, n, nthreads)
+    try:
+        adv()  # warm (Euler start)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            adv()
+        sec = time.perf_counter() - t0
+    finally:
+        restore()
     return ncell * steps / sec, sec, desc, threads
 
 
@@ -336,7 +348,7 @@ def run_reference(args):
         return 0
     n = args.n
     W = workload(args.workload, n)
-    adv, ncell, desc, threads = cpu_stepper(args.workload, n)
+    adv, ncell, desc, threads, _restore = cpu_stepper(args.workload, n)
     for _ in range(max(1, min(args.warmup, 1))):
         adv()  # untimed (includes the Euler start)
     per_step = []
@@ -806,6 +818,11 @@ def run_ours(args):
             line["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": threads, "kind": "port",
                                     "sample": f"2 steps of the workload at {g[0]}x{g[1]}x{g[2]} "
                                               f"({csec:.1f} s) after one untimed step; {desc}"}
+            if args.workload == "hit" and threads > 1:
+                sv, ssec, _, st1 = cpu_baseline_sample(args.workload, cn, 1, nthreads=1)
+                line["cpu_baseline"]["single_thread"] = {
+                    "value": sv, "cores": st1,
+                    "sample": f"1 step at {g[0]}x{g[1]}x{g[2]} ({ssec:.1f} s) after one untimed step"}
         except Exception as e:  # the baseline never blocks the GPU line
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                     "sample": f"failed: {e}"}

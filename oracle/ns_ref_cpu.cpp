@@ -302,6 +302,11 @@ struct cpu_session {
 extern "C" {
 
 int cpu_threads(void) { return omp_get_max_threads(); }
+// The host threads later steps use (n >= 1); returns the new count.
+int cpu_set_threads(int n) {
+  if (n >= 1) omp_set_num_threads(n);
+  return omp_get_max_threads();
+}
 
 cpu_session* cpu_create(int nx, int ny, int nz, double lx, double ly, double lz, double nu, double dt, int scheme,
                         int dp_flag, int gauge) {

@@ -27,6 +27,8 @@ def load():
         lib.cpu_step.argtypes = [C.c_void_p] + [_DP] * 7 + [C.c_int]
         lib.cpu_destroy.argtypes = [C.c_void_p]
         lib.cpu_threads.restype = C.c_int
+        lib.cpu_set_threads.restype = C.c_int
+        lib.cpu_set_threads.argtypes = [C.c_int]
         _lib = lib
     return _lib
 
@@ -57,6 +59,9 @@ class CpuStep:
 
     def threads(self):
         return int(self.lib.cpu_threads())
+
+    def set_threads(self, n):
+        return int(self.lib.cpu_set_threads(int(n)))
 
     def close(self):
         if self.h:
