@@ -16,14 +16,9 @@
 
 namespace ns {
 
-__device__ __forceinline__ void correct_body(const CorrectArgs& a, long long t) {
+// Slot (i, j, k) of the padded box.
+__device__ __forceinline__ void correct_body(const CorrectArgs& a, int i, int j, int k) {
   const Layout L = a.L;
-  const int nx2 = L.nx + 2, ny2 = L.ny + 2, nz2 = L.nz + 2;
-  const long long tot = (long long)nx2 * ny2 * nz2;
-  if (t >= tot) return;
-  const int i = (int)(t % nx2);
-  const int j = (int)((t / nx2) % ny2);
-  const int k = (int)(t / ((long long)nx2 * ny2));
   const FOne c{a.one, a.mzero};
   const long long g = L.at(i, j, k);
   const double* __restrict__ dp = a.dp;
@@ -60,10 +55,22 @@ __device__ __forceinline__ void correct_body(const CorrectArgs& a, long long t) 
   }
 }
 
-// Slots t in [t0, t1) of the padded box (x fastest).
-__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a, long long t0, long long t1) {
-  const long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t < t1) correct_body(a, t);
+// Flat slot index t of the padded box (x fastest).
+__device__ __forceinline__ void correct_body(const CorrectArgs& a, long long t) {
+  const Layout L = a.L;
+  const int nx2 = L.nx + 2, ny2 = L.ny + 2, nz2 = L.nz + 2;
+  if (t >= (long long)nx2 * ny2 * nz2) return;
+  correct_body(a, (int)(t % nx2), (int)((t / nx2) % ny2), (int)(t / ((long long)nx2 * ny2)));
+}
+
+// Plane k0 + blockIdx.y; the x blocks cover its (nx+2)(ny+2) slots, which a
+// 32-bit division splits into (i, j).
+__global__ void __launch_bounds__(256) correct_kernel(CorrectArgs a, int k0) {
+  const unsigned nx2 = (unsigned)a.L.nx + 2u;
+  const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nx2 * ((unsigned)a.L.ny + 2u)) return;
+  const unsigned j = q / nx2;
+  correct_body(a, (int)(q - j * nx2), (int)j, k0 + (int)blockIdx.y);
 }
 
 // Batched: one 256-element chunk of a subdomain box per work item.
@@ -90,8 +97,8 @@ cudaError_t launch_correct_planes(const CorrectArgs& a, int k0, int k1, cudaStre
   if (k0 < 0 || k1 > a.L.nz + 2 || k0 > k1) return cudaErrorInvalidValue;
   if (k0 == k1) return cudaSuccess;
   const long long plane = (long long)(a.L.nx + 2) * (a.L.ny + 2);
-  const long long n = plane * (k1 - k0);
-  correct_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, plane * k0, plane * k1);
+  const dim3 grid((unsigned)((plane + 255) / 256), (unsigned)(k1 - k0));
+  correct_kernel<<<grid, 256, 0, st>>>(a, k0);
   return cudaGetLastError();
 }
 
