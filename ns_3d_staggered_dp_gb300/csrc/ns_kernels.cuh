@@ -68,16 +68,18 @@ bool make_pred_tma(PredTma& t, const Layout& L, const double* u, const double* v
 
 // Combine the stencil pieces into u* and rewrite the AB2 history at g.
 template <int SCHEME, bool FIRST>
+// prev is hist[g] (read by the caller ahead of time; unused for Euler and
+// the first step).
 __device__ __forceinline__ double predictor_combine(const PredictArgs& a, const FOne& c, double uc, double sWE,
-                                                    double sSN, double sBT, double C, double* __restrict__ hist,
-                                                    long long g) {
+                                                    double sSN, double sBT, double C, double prev,
+                                                    double* __restrict__ hist, long long g) {
   if (SCHEME == 2) {  // AB2-CN explicit half (big_periodic_3D.f90:398-423)
     double t = fmul(c, a.c0, uc);
     t = fma(a.ca, sWE, t);
     t = fma(a.cb, sSN, t);
     t = fma(a.cc, sBT, t);
     t = fma(FIRST ? a.dt : a.cC, C, t);  // Euler start: rhs = nu/2 diff - conv (big_periodic_3D.f90:400-408)
-    if (!FIRST) t = fma(a.cP, hist[g], t);
+    if (!FIRST) t = fma(a.cP, prev, t);
     hist[g] = C;  // rhs_?_previous = -conv
     return t;
   } else {
@@ -87,7 +89,7 @@ __device__ __forceinline__ double predictor_combine(const PredictArgs& a, const 
     rhs = fma(a.kx, sWE, rhs);  // nu*diff - conv
     double t;
     if (SCHEME == 1 && !FIRST) {  // AB2 (big_periodic_3D.f90:369-396)
-      t = fma(a.e2, hist[g], uc);
+      t = fma(a.e2, prev, uc);
       t = fma(a.e1, rhs, t);
     } else {  // Euler, or the Euler start of AB2
       t = fma(a.dt, rhs, uc);

@@ -256,6 +256,18 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
   for (int k = k0; k < k1; ++k) {
     const int s0 = k & 3, s1 = (k + 1) & 3, sm = (k + 3) & 3;  // planes k, k+1, k-1
     const int pb = k & 1, pbm = (k - 1) & 1;
+    // With the tile loader, this cell's AB2 history is read before the
+    // plane's waits so that its latency overlaps them (each cell's history is
+    // read and then rewritten by its own thread only); read where it is used,
+    // it left the tile-loader kernel at 3.3 ms against 2.1.  The cp.async
+    // loader reads it at the combine (its copies already fill that time).
+    double pu = 0.0, pv = 0.0, pw = 0.0;
+    if (TMA && MODE == 0 && SCHEME != 0 && !FIRST && in_xy) {
+      const long long gh = L.at(i, j, k);
+      pu = __ldg(a.hx + gh);
+      pv = __ldg(a.hy + gh);
+      pw = __ldg(a.hz + gh);
+    }
     // plane k+1 has landed and every thread is done with plane k-2, whose
     // slot receives plane k+2 while this plane is computed
     if (TMA) wait_slot((k + 1) & 3);
@@ -296,7 +308,7 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
         } else if (MODE == 2) {
           out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, uc))));
         } else {
-          out = predictor_combine<SCHEME, FIRST>(a, c, uc, sWE, sSN, sBT, C, a.hx, g);
+          out = predictor_combine<SCHEME, FIRST>(a, c, uc, sWE, sSN, sBT, C, TMA ? pu : a.hx[g], a.hx, g);
           if (DPF) out = fma(a.gpx, fsub(c, __ldg(a.p + g), __ldg(a.p + g - 1)), out);
         }
         a.us[g] = out;
@@ -322,7 +334,7 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
         } else if (MODE == 2) {
           out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, vc))));
         } else {
-          out = predictor_combine<SCHEME, FIRST>(a, c, vc, sWE, sSN, sBT, C, a.hy, g);
+          out = predictor_combine<SCHEME, FIRST>(a, c, vc, sWE, sSN, sBT, C, TMA ? pv : a.hy[g], a.hy, g);
           if (DPF) out = fma(a.gpy, fsub(c, __ldg(a.p + g), __ldg(a.p + g - L.sy)), out);
         }
         a.vs[g] = out;
@@ -348,7 +360,7 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
         } else if (MODE == 2) {
           out = fma(a.ix2, sWE, fma(a.iy2, sSN, fma(a.iz2, sBT, fmul(c, a.lap0, wc))));
         } else {
-          out = predictor_combine<SCHEME, FIRST>(a, c, wc, sWE, sSN, sBT, C, a.hz, g);
+          out = predictor_combine<SCHEME, FIRST>(a, c, wc, sWE, sSN, sBT, C, TMA ? pw : a.hz[g], a.hz, g);
           if (DPF) out = fma(a.gpz, fsub(c, __ldg(a.p + g), __ldg(a.p + g - L.sz)), out);
         }
         a.ws[g] = out;
