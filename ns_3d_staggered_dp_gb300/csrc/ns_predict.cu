@@ -253,20 +253,27 @@ __device__ __forceinline__ void predict_body(const PredictArgs& a, PredSmem& S, 
   const bool act_u = in_xy && (i >= a.ulo);
   const bool act_v = in_xy && (j >= a.vlo);
 
+  double hu = 0.0, hv = 0.0, hw = 0.0;  // tile loader: the AB2 history of this cell at plane k
+  if (TMA && MODE == 0 && SCHEME != 0 && !FIRST && in_xy && k0 < k1) {
+    const long long gh = L.at(i, j, k0);
+    hu = __ldg(a.hx + gh);
+    hv = __ldg(a.hy + gh);
+    hw = __ldg(a.hz + gh);
+  }
   for (int k = k0; k < k1; ++k) {
     const int s0 = k & 3, s1 = (k + 1) & 3, sm = (k + 3) & 3;  // planes k, k+1, k-1
     const int pb = k & 1, pbm = (k - 1) & 1;
-    // With the tile loader, this cell's AB2 history is read before the
-    // plane's waits so that its latency overlaps them (each cell's history is
-    // read and then rewritten by its own thread only); read where it is used,
-    // it left the tile-loader kernel at 3.3 ms against 2.1.  The cp.async
-    // loader reads it at the combine (its copies already fill that time).
-    double pu = 0.0, pv = 0.0, pw = 0.0;
-    if (TMA && MODE == 0 && SCHEME != 0 && !FIRST && in_xy) {
-      const long long gh = L.at(i, j, k);
-      pu = __ldg(a.hx + gh);
-      pv = __ldg(a.hy + gh);
-      pw = __ldg(a.hz + gh);
+    // With the tile loader, this cell's AB2 history is read one plane
+    // ahead, so that its latency overlaps a whole iteration (each cell's
+    // history is read and then rewritten by its own thread only); read where
+    // it is used, it left the tile-loader kernel at 3.3 ms against 2.1.  The
+    // cp.async loader reads it at the combine (its copies already fill that time).
+    const double pu = hu, pv = hv, pw = hw;
+    if (TMA && MODE == 0 && SCHEME != 0 && !FIRST && in_xy && k + 1 < k1) {
+      const long long gh = L.at(i, j, k + 1);  // the next plane's, one iteration ahead
+      hu = __ldg(a.hx + gh);
+      hv = __ldg(a.hy + gh);
+      hw = __ldg(a.hz + gh);
     }
     // plane k+1 has landed and every thread is done with plane k-2, whose
     // slot receives plane k+2 while this plane is computed
