@@ -43,8 +43,18 @@ module ns_gpu
   type, bind(C) :: ns_batch_config
     integer(c_int) :: scheme, bc, pbc, restart, n_slots, mode, use_graph
     real(c_double) :: nu, dt0, dx, dy, dz
-    integer(c_int) :: grid(16), reserved(8)
+    integer(c_int) :: grid(16)
+    integer(c_int) :: using_ustar   ! 1: faces from the parent's u*; 0: from u (+ dt grad p_prev when dp_flag = 0)
+    integer(c_int) :: dp_flag       ! 1: incremental pressure; 0: p = dp
+    integer(c_int) :: reserved(6)
   end type ns_batch_config
+
+  ! Per-kernel device time of ns_profile (the SYSTEM_CLOCK phases of big_periodic_3D.f90:328-569).
+  type, bind(C) :: ns_kernel_time
+    character(kind=c_char) :: name(32)
+    real(c_double) :: ms
+    integer(c_long_long) :: launches
+  end type ns_kernel_time
 
   interface
     integer(c_int) function ns_config_default(cfg, nx, ny, nz) bind(C, name="ns_config_default")
@@ -60,6 +70,32 @@ module ns_gpu
     end function
 
     integer(c_int) function ns_destroy(h) bind(C, name="ns_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    ! C strings: convert with ns_string (below)
+    type(c_ptr) function ns_last_error(h) bind(C, name="ns_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    type(c_ptr) function ns_status_string(status) bind(C, name="ns_status_string")
+      import :: c_ptr, c_int
+      integer(c_int), value :: status
+    end function
+
+    type(c_ptr) function ns_version() bind(C, name="ns_version")
+      import :: c_ptr
+    end function
+
+    integer(c_int) function ns_set_stream(h, stream) bind(C, name="ns_set_stream")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      type(c_ptr), value :: stream               ! cudaStream_t
+    end function
+
+    integer(c_int) function ns_synchronize(h) bind(C, name="ns_synchronize")
       import :: c_int, c_ptr
       type(c_ptr), value :: h
     end function
@@ -103,6 +139,46 @@ module ns_gpu
       import :: c_int, c_ptr, ns_diag
       type(c_ptr), value :: h
       type(ns_diag), intent(out) :: d
+    end function
+
+    ! u_star, v_star, w_star, dp of the last step (the sources of the sub-block records, big_periodic_3D.f90:664-712)
+    integer(c_int) function ns_get_stage(h, us, vs, ws, dp) bind(C, name="ns_get_stage")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out), optional :: us(*), vs(*), ws(*), dp(*)
+    end function
+
+    ! TGV (NS_functions.f90:18-50) on the GPU: call ns_tgv(xu, nx+1, yu, ny+2, nz+2, t, nu, u=u) etc.
+    integer(c_int) function ns_tgv(x, nx, y, ny, nz, t, nu, u, v, w, p) bind(C, name="ns_tgv")
+      import :: c_int, c_double
+      integer(c_int), value :: nx, ny, nz
+      real(c_double), intent(in) :: x(*), y(*)
+      real(c_double), value :: t, nu
+      real(c_double), intent(inout), optional :: u(*), v(*), w(*), p(*)
+    end function
+
+    integer(c_int) function ns_profile(h, nsteps, out, max_out, n_out) bind(C, name="ns_profile")
+      import :: c_int, c_ptr, ns_kernel_time
+      type(c_ptr), value :: h
+      integer(c_int), value :: nsteps, max_out
+      type(ns_kernel_time), intent(out) :: out(*)
+      integer(c_int), intent(out) :: n_out
+    end function
+
+    integer(c_int) function ns_launch_count(h, launches) bind(C, name="ns_launch_count")
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: h
+      integer(c_long_long), intent(out) :: launches
+    end function
+
+    ! The periodic FFT Poisson solve on caller-owned device arrays, allocating nothing
+    integer(c_int) function ns_poisson_fft_noalloc(rhs_dev, dp_dev, nx, ny, nz, lx, ly, lz, stream) &
+        bind(C, name="ns_poisson_fft_noalloc")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: rhs_dev, dp_dev      ! device addresses (e.g. from a CUDA Fortran or C allocator)
+      integer(c_int), value :: nx, ny, nz
+      real(c_double), value :: lx, ly, lz
+      type(c_ptr), value :: stream               ! cudaStream_t, or c_null_ptr
     end function
 
     integer(c_int) function ns_cal_conv(h, u, v, w, cx, cy, cz) bind(C, name="ns_cal_conv")
@@ -165,6 +241,79 @@ module ns_gpu
     integer(c_int) function ns_batch_destroy(b) bind(C, name="ns_batch_destroy")
       import :: c_int, c_ptr
       type(c_ptr), value :: b
+    end function
+
+    type(c_ptr) function ns_batch_last_error(b) bind(C, name="ns_batch_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: b
+    end function
+
+    integer(c_int) function ns_batch_set_stream(b, stream) bind(C, name="ns_batch_set_stream")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b, stream
+    end function
+
+    ! Initial sub-block state from host arrays (the u_sub ... groups read at
+    ! re_simulation_sub_tstep_interBC_combine.f90:421-433)
+    integer(c_int) function ns_batch_set_state(b, i, u, v, w, p, rx, ry, rz) bind(C, name="ns_batch_set_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      integer(c_int), value :: i                   ! 0-based subdomain index
+      real(c_double), intent(in) :: u(*), v(*), w(*), p(*)
+      real(c_double), intent(in), optional :: rx(*), ry(*), rz(*)
+    end function
+
+    ! A snapshot from host faces (the records read at re_simulation_sub_tstep_interBC_combine.f90:455-504,
+    ! turned into faces by get_velpr_bc): faces(k) = c_loc of the k-th get_velpr_bc output, or c_null_ptr
+    integer(c_int) function ns_batch_set_snapshot(b, slot, t, i, faces, mean_dp) bind(C, name="ns_batch_set_snapshot")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      integer(c_int), value :: slot, i
+      real(c_double), value :: t, mean_dp
+      type(c_ptr), intent(in) :: faces(24)
+    end function
+
+    integer(c_int) function ns_batch_get_snapshot(b, slot, i, faces, mean_dp) bind(C, name="ns_batch_get_snapshot")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      integer(c_int), value :: slot, i
+      type(c_ptr), intent(in) :: faces(24)         ! c_loc of the 24 output arrays, or c_null_ptr
+      real(c_double), intent(out), optional :: mean_dp
+    end function
+
+    integer(c_int) function ns_batch_launch_count(b, launches) bind(C, name="ns_batch_launch_count")
+      import :: c_int, c_ptr, c_long_long
+      type(c_ptr), value :: b
+      integer(c_long_long), intent(out) :: launches
+    end function
+
+    integer(c_int) function ns_batch_autotune(b, reps) bind(C, name="ns_batch_autotune")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b
+      integer(c_int), value :: reps
+    end function
+
+    integer(c_int) function ns_batch_profile(b, reps, ms_per_stage) bind(C, name="ns_batch_profile")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: b
+      integer(c_int), value :: reps
+      real(c_double), intent(out) :: ms_per_stage(16)
+    end function
+
+    integer(c_int) function ns_batch_get_config(b, cfg) bind(C, name="ns_batch_get_config")
+      import :: c_int, c_ptr, ns_batch_config
+      type(c_ptr), value :: b
+      type(ns_batch_config), intent(out) :: cfg
+    end function
+
+    ! interp1(knots, y, t, 'spline') weights on the 6-knot window (sub_tstep_BC_combined_interpolation.m:53-64)
+    integer(c_int) function ns_spline_weights(knots, n_knots, t, first, w) bind(C, name="ns_spline_weights")
+      import :: c_int, c_double
+      real(c_double), intent(in) :: knots(*)
+      integer(c_int), value :: n_knots
+      real(c_double), value :: t
+      integer(c_int), intent(out) :: first         ! 0-based index of the window's first knot
+      real(c_double), intent(out) :: w(6)
     end function
 
     integer(c_int) function ns_batch_init_from_parent(b, parent) bind(C, name="ns_batch_init_from_parent")
@@ -244,6 +393,120 @@ module ns_gpu
       real(c_double), intent(out), optional :: dhx(*), dhy(*), dhz(*)
     end function
 
+    ! --- HDF5 files of the reference without libhdf5 (big_periodic_3D.f90:593-726) ---
+    ! Paths and names are NUL-terminated (trim(name)//c_null_char).  dims in Fortran order.
+    integer(c_int) function ns_h5_create(path, overwrite, f) bind(C, name="ns_h5_create")       ! h5fcreate_f
+      import :: c_int, c_ptr, c_char
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: overwrite
+      type(c_ptr), intent(out) :: f
+    end function
+
+    integer(c_int) function ns_h5_open(path, writable, f) bind(C, name="ns_h5_open")           ! h5fopen_f
+      import :: c_int, c_ptr, c_char
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: writable
+      type(c_ptr), intent(out) :: f
+    end function
+
+    integer(c_int) function ns_h5_flush(f) bind(C, name="ns_h5_flush")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: f
+    end function
+
+    integer(c_int) function ns_h5_close(f) bind(C, name="ns_h5_close")                        ! h5fclose_f
+      import :: c_int, c_ptr
+      type(c_ptr), value :: f
+    end function
+
+    type(c_ptr) function ns_h5_last_error(f) bind(C, name="ns_h5_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: f
+    end function
+
+    integer(c_int) function ns_h5_group(f, path) bind(C, name="ns_h5_group")                  ! h5gcreate_f
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: path(*)
+    end function
+
+    integer(c_int) function ns_h5_attr_int(f, obj, name, value) bind(C, name="ns_h5_attr_int")  ! h5ltset_attribute_int_f
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: obj(*), name(*)
+      integer(c_int), value :: value
+    end function
+
+    integer(c_int) function ns_h5_attr_double(f, obj, name, value) bind(C, name="ns_h5_attr_double")
+      import :: c_int, c_ptr, c_char, c_double
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: obj(*), name(*)
+      real(c_double), value :: value
+    end function
+
+    integer(c_int) function ns_h5_attr_string(f, obj, name, value) bind(C, name="ns_h5_attr_string")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: obj(*), name(*), value(*)
+    end function
+
+    integer(c_int) function ns_h5_write_double(f, path, rank, dims, data) bind(C, name="ns_h5_write_double")
+      import :: c_int, c_ptr, c_char, c_double, c_long_long                           ! h5ltmake_dataset_double_f
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: rank
+      integer(c_long_long), intent(in) :: dims(*)
+      real(c_double), intent(in) :: data(*)
+    end function
+
+    integer(c_int) function ns_h5_dims(f, path, rank, dims) bind(C, name="ns_h5_dims")        ! h5ltget_dataset_info_f
+      import :: c_int, c_ptr, c_char, c_long_long
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), intent(out) :: rank
+      integer(c_long_long), intent(out) :: dims(32)
+    end function
+
+    integer(c_int) function ns_h5_read_double(f, path, rank, dims, out) bind(C, name="ns_h5_read_double")
+      import :: c_int, c_ptr, c_char, c_double, c_long_long                           ! h5ltread_dataset_double_f
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: rank
+      integer(c_long_long), intent(in) :: dims(*)
+      real(c_double), intent(out) :: out(*)
+    end function
+
+    integer(c_int) function ns_h5_get_attr_int(f, obj, name, value) bind(C, name="ns_h5_get_attr_int")
+      import :: c_int, c_ptr, c_char, c_long_long
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: obj(*), name(*)
+      integer(c_long_long), intent(out) :: value
+    end function
+
+    integer(c_int) function ns_h5_get_attr_double(f, obj, name, value) bind(C, name="ns_h5_get_attr_double")
+      import :: c_int, c_ptr, c_char, c_double
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: obj(*), name(*)
+      real(c_double), intent(out) :: value
+    end function
+
+    integer(c_int) function ns_h5_get_attr_string(f, obj, name, buf, buflen) bind(C, name="ns_h5_get_attr_string")
+      import :: c_int, c_ptr, c_char
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: obj(*), name(*)
+      character(kind=c_char), intent(out) :: buf(*)
+      integer(c_int), value :: buflen
+    end function
+
+    integer(c_int) function ns_h5_members(f, group, buf, buflen, needed) bind(C, name="ns_h5_members")
+      import :: c_int, c_ptr, c_char, c_long_long
+      type(c_ptr), value :: f
+      character(kind=c_char), intent(in) :: group(*)
+      character(kind=c_char), intent(out) :: buf(*)
+      integer(c_long_long), value :: buflen
+      integer(c_long_long), intent(out) :: needed
+    end function
+
     ! The session's state as a snapshot in the layout of big_periodic_3D.f90:630-651
     ! (no libhdf5 needed), and the restart of :309-324 from such a file.
     integer(c_int) function ns_h5_write_state(h, path, time, time_step, overwrite) bind(C, name="ns_h5_write_state")
@@ -262,4 +525,28 @@ module ns_gpu
       integer(c_int), intent(out), optional :: time_step
     end function
   end interface
+
+contains
+
+  ! A NUL-terminated C string (ns_last_error, ns_status_string, ...) as a Fortran string.
+  function ns_string(p) result(s)
+    type(c_ptr), intent(in) :: p
+    character(len=:), allocatable :: s
+    character(kind=c_char), pointer :: c(:)
+    integer :: n
+    interface
+      integer(c_size_t) function c_strlen(q) bind(C, name="strlen")
+        import :: c_size_t, c_ptr
+        type(c_ptr), value :: q
+      end function
+    end interface
+    if (.not. c_associated(p)) then
+      s = ""
+      return
+    end if
+    n = int(c_strlen(p))
+    call c_f_pointer(p, c, [n])
+    allocate(character(len=n) :: s)
+    s = transfer(c(1:n), s)
+  end function ns_string
 end module ns_gpu

@@ -152,6 +152,25 @@ int ns_step(ns_handle* h, int nsteps);
 /* max|div u| and the probe value of the current state (a synchronous call). */
 int ns_get_diag(ns_handle* h, ns_diag* d);
 
+/* The intermediate fields of the last step, in the reference shapes: u*, v*,
+ * w* (after the ADI sweeps with AB2-CN) and dp, gauge-shifted as
+ * big_periodic_3D.f90:562 shifts it (dp - dp(1,1,1) when cfg.gauge).  These
+ * are the u_star_sub, ..., dp_sub that the reference's parent run records
+ * for its sub-blocks (big_periodic_3D.f90:664-712).  Any pointer may be
+ * NULL.  Valid after ns_step; a synchronous call. */
+int ns_get_stage(ns_handle* h, double* u_star, double* v_star, double* w_star, double* dp);
+
+/* TGV (NS_functions.f90:18-50): the 2D Taylor-Green vortex at time t on the
+ * tensor grid x(1:nx) x y(1:ny) x nz planes, computed on the GPU:
+ *   u(i,j,:) =  cos(x_i) sin(y_j) e,   v(i,j,:) = -sin(x_i) cos(y_j) e,
+ *   p(i,j,:) = -(cos(2 x_i) + cos(2 y_j)) e^2 / 4,   e = exp(-2 nu t).
+ * u, v, p are host arrays (nx, ny, nz) in Fortran order; any may be NULL (the
+ * reference's absent optional arguments).  w is accepted and, as in the
+ * reference, left untouched.  The drivers call it once per staggered field
+ * with that field's coordinates (xu, yu for u; xv, yv for v; xp, yp for p). */
+int ns_tgv(const double* x, int nx, const double* y, int ny, int nz, double t, double nu, double* u, double* v,
+           double* w, double* p);
+
 /* ------------------------------------------------------------------------
  * Routine tier: one reference routine per call, host arrays in and out,
  * using the handle's configuration for shapes, bc codes and spacings.
@@ -188,20 +207,24 @@ int ns_correct(ns_handle* h, const double* u_star, const double* v_star, const d
 
 /* The periodic FFT pressure Poisson solve of ns_poisson without any device
  * allocation.  No counterpart in the reference: it serves callers that must
- * not allocate device memory (code running under CUDA stream capture, hosts
- * whose device memory is owned by another allocator, real-time loops that
- * cannot take an allocation's device synchronisation).
+ * not allocate device memory (hosts whose device memory is owned by another
+ * allocator or reserved up front, real-time loops that cannot take an
+ * allocation's device synchronisation).
  *   rhs_dev: device array (nx, ny, nz), Fortran order, 16-byte aligned,
  *            already BC-modified (periodic: none);
- *   dp_dev : device array (nx+2, ny+2, nz+2), Fortran order; the interior is
- *            the solution (zero mean) and the ghosts are the periodic copies;
+ *   dp_dev : device array (nx+2, ny+2, nz+2), Fortran order, 8-byte aligned;
+ *            the interior is the solution (zero mean) and the ghosts are
+ *            the periodic copies;
  *   stream : cudaStream_t the work is enqueued on (NULL: legacy stream).
  * All scratch (half spectrum, twiddles, 1/lambda; 4 MiB) is one static
  * device array held by every device that loads the library.  Grids are
  * limited to powers of two in [16, 64] per axis (NS_ERR_SHAPE otherwise).
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race. */
+ * (cudaGetSymbolAddress), keeps it for the life of the process, and should
+ * come before any stream capture; a device reset after it is not supported.
+ * A CUDA error already pending on the calling thread is left in place and
+ * the call returns NS_ERR_CUDA without launching.  Calls share the array:
+ * calls that overlap on the GPU race. */
 int ns_poisson_fft_noalloc(const double* rhs_dev, double* dp_dev, int nx, int ny, int nz, double lx, double ly,
                            double lz, void* stream);
 
@@ -264,7 +287,17 @@ typedef struct ns_batch_config {
   double dx, dy, dz;    /* grid spacing (the parent's)                           */
   int grid[16];         /* persistent CTAs per stage kernel (0: one wave);
                            set by ns_batch_autotune                              */
-  int reserved[8];
+  int using_ustar;      /* 1: velocity faces from the parent's u* (the default,
+                           re_simulation_sub_tstep_interBC_combine.f90:105);
+                           0: from the parent's u, plus dt0 * grad(p_previous)
+                           when dp_flag = 0 (get_velpr_bc, NS_functions.f90:
+                           434-444); needs sub_tstep = 1 (:360-363)           */
+  int dp_flag;          /* 1: incremental pressure (the default, :104): the
+                           predictor subtracts dt grad p, p += dp, pressure
+                           faces and mean from the parent's dp;
+                           0: p = dp, pressure faces and mean from the
+                           parent's p (dp_sub = p_sub, :506-508)              */
+  int reserved[6];
 } ns_batch_config;
 
 void ns_batch_config_default(ns_batch_config* c);
@@ -284,14 +317,30 @@ int ns_batch_get_state(ns_batch* b, int i, double* u, double* v, double* w, doub
                        double* hz);
 
 /* Snapshot slot `slot` at parent time t: the 24 face arrays of every
- * subdomain from the parent's last u* and dp (get_velpr_bc with using_Ustar
- * and dp_flag = 1, NS_functions.f90:414-510, and get_pr_bc :514-562) and the
- * mean of the parent's dp over each subdomain's interior (the mean_dp of
- * the DCT solve, re_simulation_sub_tstep_interBC_combine.f90:766-768). */
+ * subdomain (get_velpr_bc, NS_functions.f90:414-510, and get_pr_bc :514-562,
+ * on the parent's sub-block, u_sub = u(idx_xu, idx_yu, idx_zu),
+ * big_periodic_3D.f90:20-25) and the mean of the pressure source over each
+ * subdomain's interior (the mean_dp of the DCT solve,
+ * re_simulation_sub_tstep_interBC_combine.f90:766-768).  The sources follow
+ * the batch's using_ustar / dp_flag:
+ *   velocity: the parent's last u* (using_ustar = 1) or its current u
+ *             (using_ustar = 0; with dp_flag = 0 plus dt0 * diff(p_prev) / h,
+ *             p_prev = the parent's p at the previous ns_batch_capture of
+ *             this batch, or its current p at the first one);
+ *   pressure: the parent's last dp, gauge-shifted as the step shifts it
+ *             (dp_flag = 1), or its current p (dp_flag = 0).
+ * The arithmetic is the reference's, operation for operation, so the faces
+ * equal get_velpr_bc of the same parent arrays bit for bit. */
 int ns_batch_capture(ns_batch* b, const ns_handle* parent, int slot, double t);
 /* The same snapshot from host data for subdomain i: faces in get_velpr_bc
  * order (ns_set_faces), NULL entries zero. */
 int ns_batch_set_snapshot(ns_batch* b, int slot, double t, int i, const double* const faces[24], double mean_dp);
+/* Read back snapshot slot `slot` of subdomain i (the inverse of
+ * ns_batch_set_snapshot): the 24 faces in get_velpr_bc order and shapes
+ * (NULL entries skipped) and the mean (may be NULL).  These are the
+ * boundary arrays the reference's parent run writes to its sub-block record
+ * files (big_periodic_3D.f90:664-712). */
+int ns_batch_get_snapshot(ns_batch* b, int slot, int i, double* const faces[24], double* mean_dp);
 
 /* Advance every subdomain over one parent interval [t0, t0 + dt0]: the
  * first call takes sub_tstep sub-steps, later calls one step. */

@@ -53,7 +53,7 @@ class NSBatchConfig(C.Structure):
         ("scheme", C.c_int), ("bc", C.c_int), ("pbc", C.c_int), ("restart", C.c_int), ("n_slots", C.c_int),
         ("mode", C.c_int), ("use_graph", C.c_int),
         ("nu", C.c_double), ("dt0", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
-        ("grid", C.c_int * 16), ("reserved", C.c_int * 8),
+        ("grid", C.c_int * 16), ("using_ustar", C.c_int), ("dp_flag", C.c_int), ("reserved", C.c_int * 6),
     ]
 
 
@@ -73,6 +73,8 @@ SIGNATURES = {
     "ns_step": (C.c_int, [C.c_void_p, C.c_int]),
     "ns_step_host": (C.c_int, [C.c_void_p] + [_DP] * 14),
     "ns_get_diag": (C.c_int, [C.c_void_p, C.POINTER(NSDiag)]),
+    "ns_get_stage": (C.c_int, [C.c_void_p] + [_DP] * 4),
+    "ns_tgv": (C.c_int, [_DP, C.c_int, _DP, C.c_int, C.c_int, C.c_double, C.c_double] + [_DP] * 4),
     "ns_cal_conv": (C.c_int, [C.c_void_p] + [_DP] * 6),
     "ns_cal_diff": (C.c_int, [C.c_void_p] + [_DP] * 6),
     "ns_poisson": (C.c_int, [C.c_void_p, _DP, _DP]),
@@ -92,6 +94,7 @@ SIGNATURES = {
     "ns_batch_get_state": (C.c_int, [C.c_void_p, C.c_int] + [_DP] * 7),
     "ns_batch_capture": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double]),
     "ns_batch_set_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(_DP), C.c_double]),
+    "ns_batch_get_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(_DP), _DP]),
     "ns_batch_advance": (C.c_int, [C.c_void_p, C.c_double]),
     "ns_batch_max_div": (C.c_int, [C.c_void_p, C.c_int, _DP]),
     "ns_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),

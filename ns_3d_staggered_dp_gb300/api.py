@@ -27,6 +27,18 @@ FACE_ORDER = [  # get_velpr_bc output order (NS_functions.f90:414-420)
 ]
 
 
+def face_shapes(nx, ny, nz):
+    """Shapes of the 24 get_velpr_bc outputs (NS_functions.f90:418-421): the
+    face of field f on axis a spans f's extents on the two other axes."""
+    n = (nx, ny, nz)
+    out = {}
+    for name in FACE_ORDER:
+        a = "xyz".index(name[0])
+        f = "uvwp".index(name[2])
+        out[name] = tuple(n[b] + (1 if f == b else 2) for b in range(3) if b != a)
+    return out
+
+
 class NSError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{_lib.STATUS.get(status, status)}: {msg}")
@@ -160,6 +172,16 @@ class Session:
         return {"max_div": d.max_div, "probe": d.probe, "steps": d.steps_done,
                 "euler_start_pending": bool(d.euler_start_pending)}
 
+    def get_stage(self):
+        """u*, v*, w* and the gauge-shifted dp of the last step (ns_get_stage):
+        the u_star_sub ... dp_sub arrays the reference records."""
+        sh = self.shapes
+        out = {k: np.zeros(sh[k[0]], order="F") for k in ("us", "vs", "ws")}
+        out["dp"] = np.zeros(sh["p"], order="F")
+        self._check(self.lib.ns_get_stage(self.h, _ptr(out["us"]), _ptr(out["vs"]), _ptr(out["ws"]),
+                                          _ptr(out["dp"])))
+        return out
+
     def profile(self, nsteps=1):
         """Per-kernel device time (ms) over nsteps eager steps: {name: (ms, launches)}."""
         arr = (_lib.NSKernelTime * 64)()
@@ -282,6 +304,21 @@ class Session:
         return out
 
 
+def tgv(x, y, nz, t, nu, u=True, v=True, p=True):
+    """TGV (NS_functions.f90:18-50) on the GPU (ns_tgv): {name: (nx, ny, nz)
+    array} for the requested fields of the 2D Taylor-Green vortex at time t."""
+    lib = _lib.load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    shp = (len(x), len(y), int(nz))
+    out = {k: np.zeros(shp, order="F") for k, want in (("u", u), ("v", v), ("p", p)) if want}
+    s = lib.ns_tgv(_ptr(x), len(x), _ptr(y), len(y), int(nz), float(t), float(nu), _ptr(out.get("u")),
+                   _ptr(out.get("v")), None, _ptr(out.get("p")))
+    if s != 0:
+        raise NSError(s, "ns_tgv failed")
+    return out
+
+
 def spline_weights(knots, t):
     """(first, w[6]) of MATLAB interp1(knots, y, t, 'spline') on the 6-knot
     window (ns_spline_weights): value = sum_q w[q] * y[first + q]."""
@@ -389,6 +426,19 @@ class Batch:
             else:
                 arr[q] = None
         self._check(self.lib.ns_batch_set_snapshot(self.h, int(slot), float(t), int(i), arr, float(mean_dp)))
+
+    def get_snapshot(self, slot, i):
+        """(faces dict in FACE_ORDER names, mean) of snapshot slot `slot` of
+        subdomain i (ns_batch_get_snapshot)."""
+        _, _, _, nx, ny, nz, _ = self.subs[i]
+        fs = face_shapes(nx, ny, nz)
+        faces = {k: np.zeros(fs[k], order="F") for k in FACE_ORDER}
+        arr = (C.POINTER(C.c_double) * 24)()
+        for q, k in enumerate(FACE_ORDER):
+            arr[q] = _ptr(faces[k])
+        m = C.c_double()
+        self._check(self.lib.ns_batch_get_snapshot(self.h, int(slot), int(i), arr, C.byref(m)))
+        return faces, m.value
 
     def advance(self, t0):
         self._check(self.lib.ns_batch_advance(self.h, float(t0)))

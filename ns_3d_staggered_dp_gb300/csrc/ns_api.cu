@@ -1519,6 +1519,39 @@ int ns_get_diag(ns_handle* h, ns_diag* d) {
   return NS_OK;
 }
 
+// x[e] -= *g over a reference-shaped array (the gauge shift dp - dp(1,1,1),
+// big_periodic_3D.f90:562, applied to an exported copy).
+static __global__ void gauge_shift_kernel(double* __restrict__ x, long long n, const double* __restrict__ g) {
+  const double g0 = *g;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    x[e] = __dsub_rn(x[e], g0);
+}
+
+int ns_get_stage(ns_handle* h, double* us, double* vs, double* ws, double* dp) {
+  if (!h) return NS_ERR_ARG;
+  if (h->steps == 0) return fail(h, NS_ERR_ARG, "no step taken since ns_set_state: no u* or dp to return");
+  const ns_config& c = h->cfg;
+  const bool cn = c.scheme == NS_AB2_CN;
+  double* const dst[3] = {us, vs, ws};
+  const double* src[3] = {cn ? h->us2 : h->us, cn ? h->vs2 : h->vs, cn ? h->ws2 : h->ws};
+  for (int f = 0; f < 3; ++f)
+    if (dst[f]) NS_CUDA(h, d2h_field(h, dst[f], src[f], f));
+  if (dp) {
+    NS_CUDA(h, ensure_stage(h));
+    NS_CUDA(h, pack_launch(h, h->dp, h->stage, 3, false));
+    const long long n = (long long)(c.nx + 2) * (c.ny + 2) * (c.nz + 2);
+    if (c.gauge) {
+      gauge_shift_kernel<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, h->stream>>>(
+          h->stage, n, h->dp + h->L.at(0, 0, 0));
+      NS_CUDA(h, cudaGetLastError());
+      ++h->launches;
+    }
+    NS_CUDA(h, cudaMemcpyAsync(dp, h->stage, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Routine tier
 // ---------------------------------------------------------------------------

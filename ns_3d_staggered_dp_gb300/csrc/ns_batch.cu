@@ -99,15 +99,20 @@ __global__ void __launch_bounds__(kChunk) interp_kernel(const SubGeo* __restrict
   }
 }
 
-// Faces of every subdomain from the parent's u*, dp (get_velpr_bc with
-// using_Ustar, dp_flag = 1, NS_functions.f90:414-510; get_pr_bc :514-562).
-// Element e of a subdomain's face buffer is decoded to (axis a, field f,
-// side, slot s1, s2 of the plane); the reference face array index is the
-// slot minus the field's slot offset on that axis.
+// Faces of every subdomain from the parent's fields (get_velpr_bc,
+// NS_functions.f90:414-510; get_pr_bc :514-562).  pu/pv/pw are the parent's
+// u* (using_Ustar) or u, pdp its dp (dp_flag = 1) or p; pprev, when not null,
+// is the previous p whose dt*diff(pprev)/h the u branch adds with dp_flag = 0
+// (:434-437).  Element e of a subdomain's face buffer is decoded to (axis a,
+// field f, side, slot s1, s2 of the plane); the reference face array index is
+// the slot minus the field's slot offset on that axis.  Every value is formed
+// with the reference's operations in its order (no contraction into FMAs), so
+// the faces equal get_velpr_bc of the same arrays bit for bit.
 __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restrict__ geo,
                                                          const BatchItem* __restrict__ items, int n_items, Layout Lp,
                                                          const double* __restrict__ pus, const double* __restrict__ pvs,
                                                          const double* __restrict__ pws, const double* __restrict__ pdp,
+                                                         const double* __restrict__ pprev, double dt,
                                                          double* __restrict__ slot_base, int bc, int pbc, double dx,
                                                          double dy, double dz, const double* __restrict__ gauge) {
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -171,14 +176,24 @@ __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restric
     }
     // the recorded dp is the gauge-shifted one, dp - dp(1,1,1) (big_periodic_3D.f90:562)
     const double g0 = (f == 3 && gauge) ? *gauge : 0.0;
-    const double v0 = F[Lp.at(sa[0], sa[1], sa[2])] - g0;
+    // u_bc_corr = u_bc + diff(p_previous)/h*dt on the velocity fields (u branch, dp_flag = 0):
+    // diff(p) at the face slot s of field f is p[s] - p[s - e_f] in the slot layout
+    const bool corr = pprev && f < 3;
+    const double hf = f == 0 ? dx : (f == 1 ? dy : dz);
+    const long long ef = f == 0 ? 1 : (f == 1 ? Lp.sy : Lp.sz);
+    auto val = [&](const int* s) {
+      const long long q = Lp.at(s[0], s[1], s[2]);
+      if (corr) return __dadd_rn(F[q], __dmul_rn(__ddiv_rn(__dsub_rn(pprev[q], pprev[q - ef]), hf), dt));
+      return f == 3 && gauge ? __dsub_rn(F[q], g0) : F[q];
+    };
+    const double v0 = val(sa);
     double v;
     if (op == 0) {
       v = v0;
     } else {
-      const double v1 = F[Lp.at(sb[0], sb[1], sb[2])] - g0;
+      const double v1 = val(sb);
       const double h = a == 0 ? dx : (a == 1 ? dy : dz);
-      v = (op == 1) ? (v0 + v1) / 2 : (v0 - v1) / h;
+      v = (op == 1) ? __ddiv_rn(__dadd_rn(v0, v1), 2.0) : __ddiv_rn(__dsub_rn(v0, v1), h);
     }
     *out = v;
   }
@@ -368,6 +383,9 @@ struct ns_batch {
   std::map<int, cudaGraphExec_t> graphs;  // key: set * 2 + first
   std::map<int, long long> graph_count;
   cudaEvent_t copy_done = nullptr;
+  // u branch with dp_flag = 0: the parent's p at the previous capture
+  double* p_prev = nullptr;
+  long long p_prev_n = 0;
 };
 
 namespace {
@@ -414,7 +432,7 @@ cudaError_t launch_stage_kernel(ns_batch* b, int set, int stage, bool first, cud
         e = cudaGetLastError();
         break;
       case ST_PREDICT:
-        e = launch_predict_batch(b->d_pred[v], p, cnt, c.scheme, first, true, want > 0 ? grid : 0, st);
+        e = launch_predict_batch(b->d_pred[v], p, cnt, c.scheme, first, c.dp_flag != 0, want > 0 ? grid : 0, st);
         break;
       case ST_HIST:
         hist_kernel<<<grid, kChunk, 0, st>>>(b->d_geo, p, cnt);
@@ -547,6 +565,8 @@ void ns_batch_config_default(ns_batch_config* c) {
   c->n_slots = 16;
   c->mode = 0;
   c->use_graph = 1;
+  c->using_ustar = 1;
+  c->dp_flag = 1;
 }
 
 const char* ns_batch_last_error(const ns_batch* b) { return b ? b->err.c_str() : "null batch"; }
@@ -560,6 +580,7 @@ int ns_batch_destroy(ns_batch* b) {
   if (b->tri_tab) cudaFree(b->tri_tab);
   if (b->snaps) cudaFree(b->snaps);
   if (b->snap_mean) cudaFree(b->snap_mean);
+  if (b->p_prev) cudaFree(b->p_prev);
   if (b->dev_args) cudaFree(b->dev_args);
   if (b->dev_slots) cudaFree(b->dev_slots);
   if (b->dev_wts) cudaFree(b->dev_wts);
@@ -581,6 +602,8 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   else if (c.bc != 2 && c.bc != 4) msg = "batched velocity bc must be 2 or 4";
   else if (c.pbc < 2 || c.pbc > 4) msg = "batched pressure bc must be 2, 3 or 4";
   else if (c.n_slots < 1) msg = "n_slots must be >= 1";
+  else if ((c.using_ustar != 0 && c.using_ustar != 1) || (c.dp_flag != 0 && c.dp_flag != 1))
+    msg = "using_ustar and dp_flag are 0 or 1";
   else if (!(c.dt0 > 0) || !(c.nu >= 0) || !(c.dx > 0) || !(c.dy > 0) || !(c.dz > 0)) msg = "nu, dt0, dx, dy, dz";
   for (int i = 0; i < n && msg.empty(); ++i) {
     const ns_subdomain& d = subs[i];
@@ -589,6 +612,8 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     else if (d.sub_tstep < 1 || (d.sub_tstep > 1 && c.scheme != NS_AB2))
       msg = "sub_tstep >= 1 (> 1 only with AB2, re_simulation_sub_tstep_interBC_combine.f90:357-359)";
     else if (d.x0 < 1 || d.y0 < 1 || d.z0 < 1) msg = "subdomain origins are 1-based";
+    else if (!c.using_ustar && d.sub_tstep != 1)
+      msg = "sub_tstep > 1 needs u* boundary values (re_simulation_sub_tstep_interBC_combine.f90:360-363)";
   }
   if (!msg.empty()) {
     std::fprintf(stderr, "ns_batch_create: %s\n", msg.c_str());
@@ -777,7 +802,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
       ca.L = L; ca.us = us; ca.vs = vs; ca.ws = ws; ca.dp = dp;
       ca.u = g.fld[0]; ca.v = g.fld[1]; ca.w = g.fld[2]; ca.p = g.fld[3];
       ca.gx = -dt / c.dx; ca.gy = -dt / c.dy; ca.gz = -dt / c.dz;
-      ca.dp_flag = 1; ca.gauge = 0;
+      ca.dp_flag = c.dp_flag; ca.gauge = 0;
       ca.per[0] = ca.per[1] = ca.per[2] = 0;
       ca.one = 1.0; ca.mzero = -0.0;
     }
@@ -975,21 +1000,38 @@ int ns_batch_capture(ns_batch* b, const ns_handle* parent, int slot, double t) {
     if (d.x0 + d.nx > Lp.nx + 1 || d.y0 + d.ny > Lp.ny + 1 || d.z0 + d.nz > Lp.nz + 1)
       return bfail(b, NS_ERR_SHAPE, "subdomain " + std::to_string(i) + " does not fit inside the parent");
   }
+  const ns_batch_config& c = b->cfg;
   const bool cn = parent->cfg.scheme == NS_AB2_CN;
-  const double* pus = cn ? parent->us2 : parent->us;
-  const double* pvs = cn ? parent->vs2 : parent->vs;
-  const double* pws = cn ? parent->ws2 : parent->ws;
-  const double* gauge = parent->cfg.gauge ? parent->dp + Lp.at(0, 0, 0) : nullptr;
+  const double* pus = c.using_ustar ? (cn ? parent->us2 : parent->us) : parent->u;
+  const double* pvs = c.using_ustar ? (cn ? parent->vs2 : parent->vs) : parent->v;
+  const double* pws = c.using_ustar ? (cn ? parent->ws2 : parent->ws) : parent->w;
+  // pressure source: dp (gauge-shifted as the step shifts it) or p, which holds the shift already
+  const double* psrc = c.dp_flag ? parent->dp : parent->p;
+  const double* gauge = (c.dp_flag && parent->cfg.gauge) ? parent->dp + Lp.at(0, 0, 0) : nullptr;
+  const bool corr = !c.using_ustar && !c.dp_flag;
+  if (corr && b->p_prev_n != Lp.fsize) {  // first capture from this parent: p_prev = the current p
+    if (b->p_prev) cudaFree(b->p_prev);
+    b->p_prev = nullptr;
+    b->p_prev_n = 0;
+    NB_CUDA(b, cudaMalloc(&b->p_prev, (size_t)Lp.fsize * sizeof(double)));
+    b->p_prev_n = Lp.fsize;
+    NB_CUDA(b, cudaStreamSynchronize(parent->stream));
+    NB_CUDA(b, cudaMemcpyAsync(b->p_prev, parent->p, (size_t)Lp.fsize * sizeof(double), cudaMemcpyDeviceToDevice,
+                               b->stream));
+  }
   cudaEvent_t ev;
   NB_CUDA(b, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   cudaEventRecord(ev, parent->stream);
   cudaStreamWaitEvent(b->stream, ev, 0);
   const ns_batch::Range& r = b->capture_rng;
   capture_kernel<<<persistent_grid(0, r.cnt), kChunk, 0, b->stream>>>(
-      b->d_geo, b->d_items + r.off, r.cnt, Lp, pus, pvs, pws, parent->dp, b->snaps + (size_t)slot * b->slot_stride,
-      b->cfg.bc, b->cfg.pbc, b->cfg.dx, b->cfg.dy, b->cfg.dz, gauge);
-  capture_mean_kernel<<<std::min(b->n, 1024), 256, 0, b->stream>>>(b->d_geo, b->n, Lp, parent->dp,
+      b->d_geo, b->d_items + r.off, r.cnt, Lp, pus, pvs, pws, psrc, corr ? b->p_prev : nullptr, c.dt0,
+      b->snaps + (size_t)slot * b->slot_stride, c.bc, c.pbc, c.dx, c.dy, c.dz, gauge);
+  capture_mean_kernel<<<std::min(b->n, 1024), 256, 0, b->stream>>>(b->d_geo, b->n, Lp, psrc,
                                                                    b->snap_mean + (size_t)slot * b->n, gauge);
+  if (corr) {  // this capture's p is the next capture's p_previous
+    cudaMemcpyAsync(b->p_prev, parent->p, (size_t)Lp.fsize * sizeof(double), cudaMemcpyDeviceToDevice, b->stream);
+  }
   b->launches += 2;
   cudaError_t e = cudaGetLastError();
   cudaEventRecord(ev, b->stream);
@@ -1034,6 +1076,41 @@ int ns_batch_set_snapshot(ns_batch* b, int slot, double t, int i, const double* 
   NB_CUDA(b, cudaStreamSynchronize(b->stream));
   b->snap_t[slot] = t;
   b->snap_ok[slot] = 1;
+  return NS_OK;
+}
+
+int ns_batch_get_snapshot(ns_batch* b, int slot, int i, double* const faces[24], double* mean_dp) {
+  if (!b || !faces || slot < 0 || slot >= b->cfg.n_slots || i < 0 || i >= b->n) return NS_ERR_ARG;
+  if (!b->snap_ok[slot]) return bfail(b, NS_ERR_ARG, "snapshot slot " + std::to_string(slot) + " is empty");
+  const SubGeo& g = b->geo[i];
+  const Layout& L = g.L;
+  std::vector<double> buf((size_t)g.face_n, 0.0);
+  double m = 0.0;
+  NB_CUDA(b, cudaMemcpyAsync(buf.data(), b->snaps + (size_t)slot * b->slot_stride + g.snap_off,
+                             buf.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  NB_CUDA(b, cudaMemcpyAsync(&m, b->snap_mean + (size_t)slot * b->n + i, sizeof(double), cudaMemcpyDeviceToHost,
+                             b->stream));
+  NB_CUDA(b, cudaStreamSynchronize(b->stream));
+  size_t off[3][4][2];
+  {
+    size_t o = 0;
+    for (int a = 0; a < 3; ++a)
+      for (int f = 0; f < 4; ++f)
+        for (int s = 0; s < 2; ++s) { off[a][f][s] = o; o += (size_t)plane_n1(L, a) * plane_n2(L, a); }
+  }
+  for (int k = 0; k < 24; ++k) {
+    double* dst = faces[k];
+    if (!dst) continue;
+    const int f = k / 6, a = (k % 6) / 2, s = k % 2;
+    const int a1 = a == 0 ? 1 : 0, a2 = a == 2 ? 1 : 2;
+    const int e1 = field_ext(L, f, a1), e2 = field_ext(L, f, a2);
+    const int o1 = f == a1 ? 1 : 0, o2 = f == a2 ? 1 : 0;
+    const int n1 = plane_n1(L, a);
+    const double* plane = buf.data() + off[a][f][s];
+    for (int q = 0; q < e2; ++q)
+      for (int r = 0; r < e1; ++r) dst[r + (size_t)e1 * q] = plane[(size_t)(r + o1) + (size_t)n1 * (q + o2)];
+  }
+  if (mean_dp) *mean_dp = m;
   return NS_OK;
 }
 

@@ -2,12 +2,11 @@
 // its scratch (half spectrum, twiddle tables, inverse eigenvalues) in one
 // file-scope device array, for callers that must not allocate device memory.
 //
-// Who cannot allocate: code that runs while a stream is being captured into
-// a CUDA graph (cudaMalloc is not a stream operation and synchronises the
-// device), solvers embedded in a host application whose device memory is
-// wholly owned by another allocator (a framework's caching pool or a
-// pre-reserved arena), and real-time loops that cannot take the implicit
-// device synchronisation and latency of an allocation.
+// Who cannot allocate: solvers embedded in a host application whose device
+// memory is wholly owned by another allocator (a framework's caching pool,
+// or an arena the host reserved up front so that nothing else may take
+// device memory), and real-time loops that cannot take the implicit device
+// synchronisation and latency of an allocation.
 //
 // Limits and rules:
 //  - The scratch is kNoAllocScratchDoubles doubles (4 MiB) in every device
@@ -17,8 +16,12 @@
 //    64 x 64 x 64 (powers of two, each in [16, 64]) fit.  Larger grids are
 //    rejected with NS_ERR_SHAPE.
 //  - The device address of the array is looked up with cudaGetSymbolAddress
-//    on the first call on each device (with that device current).  Make that
-//    first call before any stream capture.
+//    on the first call on each device (with that device current) and kept
+//    for the life of the process.  Make that first call before any stream
+//    capture.  A device reset (cudaDeviceReset) after it is not supported:
+//    the module is reloaded and the kept address is stale.
+//  - A CUDA error already pending on the calling thread is left in place:
+//    the call then returns NS_ERR_CUDA without launching anything.
 //  - All calls share the array and it keeps the last call's contents; the
 //    tables are rebuilt by every call and the spectrum is fully overwritten,
 //    so nothing has to start at zero.  Calls that overlap on the GPU (two
@@ -82,7 +85,8 @@ bool pow2_in(int n, int lo, int hi) { return n >= lo && n <= hi && (n & (n - 1))
 
 extern "C" int ns_poisson_fft_noalloc(const double* rhs_dev, double* dp_dev, int nx, int ny, int nz, double lx,
                                       double ly, double lz, void* stream) {
-  if (!rhs_dev || !dp_dev || !(lx > 0) || !(ly > 0) || !(lz > 0) || ((uintptr_t)rhs_dev & 15)) {
+  if (!rhs_dev || !dp_dev || !(lx > 0) || !(ly > 0) || !(lz > 0) || ((uintptr_t)rhs_dev & 15) ||
+      ((uintptr_t)dp_dev & 7)) {
     std::fprintf(stderr, "ns_poisson_fft_noalloc: null or misaligned pointer, or non-positive length\n");
     return NS_ERR_ARG;
   }
@@ -98,6 +102,12 @@ extern "C" int ns_poisson_fft_noalloc(const double* rhs_dev, double* dp_dev, int
   const size_t n_tw = (size_t)(M + M / 2 + 1 + ny + nz) * 2;
   if (n_spec + n_lam + n_tw > kNoAllocScratchDoubles) return NS_ERR_SHAPE;
 
+  // An error left by the caller's earlier work is not ours to consume: report it, launch nothing.
+  if (cudaPeekAtLastError() != cudaSuccess) {
+    std::fprintf(stderr, "ns_poisson_fft_noalloc: a CUDA error is already pending: %s\n",
+                 cudaGetErrorString(cudaPeekAtLastError()));
+    return NS_ERR_CUDA;
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return NS_ERR_CUDA;
   double* base;

@@ -1163,3 +1163,35 @@ def resimulate(st, cfg, knot_t, knot_data, t_start, n_intervals, sub_tstep=1, re
             if nsub > 1 and s == nsub:
                 st.px, st.py, st.pz = (a.copy() for a in saved)
     return st
+
+
+def resimulate_frames(st, cfg, frames, p_prev0, using_ustar=True, dp_flag=1, restart=True):
+    """Re-simulate one sub-block stepped at the parent's own time step, one
+    parent record per step, with either boundary source of
+    re_simulation_sub_tstep_interBC_combine.f90:436-519.
+
+    ``frames[m]`` is the parent's sub-block after parent step m+1: a dict with
+    u, v, w, p (u_sub ... p_sub) and us, vs, ws, dp (u_star_sub ... dp_sub).
+    ``p_prev0`` is p_sub of the record before frames[0].  Per step, as the
+    reference's loop does: p_sub_pre = p_sub (:439-441); dp_sub = p_sub when
+    dp_flag = 0 (:506-508); faces from get_velpr_bc on u*_sub (using_Ustar)
+    or u_sub (:510-520), whose u branch adds dt * diff(p_sub_pre) / h with
+    dp_flag = 0 (NS_functions.f90:434-437); the DCT solve with the mean of
+    dp_sub (:766-768); p = dp_flag * p + dp (:801).
+    """
+    dx, dy, dz = cfg.h
+    st = st.copy()
+    st.first = not restart
+    p_sub_pre = p_prev0
+    for fr in frames:
+        dp_sub = fr["dp"] if dp_flag else fr["p"]
+        if using_ustar:
+            faces = get_velpr_bc(fr["us"], fr["vs"], fr["ws"], dp_sub, cfg.bc, cfg.pbc, dx, dy, dz, cfg.dt, dp_flag,
+                                 True, p_sub_pre)
+        else:
+            faces = get_velpr_bc(fr["u"], fr["v"], fr["w"], dp_sub, cfg.bc, cfg.pbc, dx, dy, dz, cfg.dt, dp_flag,
+                                 False, p_sub_pre)
+        c = dataclasses.replace(cfg, mean_dp=float(np.mean(dp_sub[1:-1, 1:-1, 1:-1])), gauge=0, dp_flag=dp_flag)
+        st = step(st, c, faces=faces)
+        p_sub_pre = fr["p"]
+    return st

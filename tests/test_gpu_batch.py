@@ -220,3 +220,19 @@ def test_error_metrics_session_and_batch_match_the_oracle():
                 parent_sub = [O.extract_sub(full[k], k, maps) for k in ("u", "v", "w", "p")]
                 ref = O.error_metrics(sd["u"], sd["v"], sd["w"], sd["p"], *parent_sub, h, h)
                 assert np.allclose(got[i], ref, rtol=1e-12, atol=0), (i, got[i], ref)
+
+
+def test_batch_bench_set_of_64_boxes_matches_oracle():
+    """The 64 sub-blocks the batched bench runs (edges from {16, 24, 32, 48,
+    64} per axis, sub-step ratios {1, 2, 4}, seed 4096) against the oracle's
+    re-simulation of each: the first parent interval with its sub-steps and
+    one regular interval, restarted AB2 from a given history."""
+    import bench
+    subs = bench.resim_subdomains()
+    assert {s[3] for s in subs} | {s[4] for s in subs} | {s[5] for s in subs} >= {48, 64}
+    assert {s[6] for s in subs} == {1, 2, 4}
+    got, refs, _ = run_case(subs, True, n_intervals=2, stride=1)
+    for i, (g, r) in enumerate(zip(got, refs)):
+        for k, rr in (("u", r.u), ("v", r.v), ("w", r.w), ("p", r.p)):
+            err = rel_l2(g[k], rr)
+            assert err < STEP_TOL, (i, subs[i], k, err)

@@ -1,10 +1,16 @@
-"""Parity at the full size of the headline workload: the 256^3 periodic
-AB2-CN step on the GPU against the C++/OpenMP restatement of the reference
-step (oracle/ns_ref_cpu.cpp, itself checked against the NumPy oracle), 3
-steps from an Euler start on a seeded solenoidal field of unit rms.
+"""Parity at the full sizes of the workloads the step is quoted on.
 
-Tolerance: relative L2 1e-10 per field (the step's parity bound) and
-max|div u| <= 1e-12 after the steps."""
+- 256^3 periodic decaying turbulence, AB2-CN: the GPU against the C++/OpenMP
+  restatement of the reference step (oracle/ns_ref_cpu.cpp, itself checked
+  against the NumPy oracle), 10 steps from an Euler start on a seeded
+  solenoidal field of unit rms.
+- 256x128x256 wall-bounded box (x, z periodic; y no-slip walls, Neumann
+  pressure), AB2-CN, Re = 180, dt = 2e-3: the GPU against the NumPy oracle,
+  10 steps from the laminar profile plus a seeded divergence-free
+  perturbation of amplitude 0.05.
+
+Tolerance: relative L2 1e-10 per field after the 10 steps (the step's parity
+bound) and max|div u| <= 1e-12."""
 import numpy as np
 import pytest
 
@@ -35,7 +41,7 @@ def solenoidal_field(n, seed):
     return st
 
 
-def test_256_cubed_three_steps_match_the_cpu_restatement():
+def test_256_cubed_ten_steps_match_the_cpu_restatement():
     from ns_3d_staggered_dp_gb300 import Session, make_config
     from oracle.ns_ref_cpu import CpuStep
     n = 256
@@ -45,13 +51,37 @@ def test_256_cubed_three_steps_match_the_cpu_restatement():
     cfg = O.Config(n, n, n, nu=1.0 / 1600.0, dt=dt, scheme=O.AB2_CN)
     ref = st.copy()
     cpu = CpuStep(cfg)
-    for _ in range(3):
+    for _ in range(10):
         cpu.step(ref)
     with Session(make_config(n, n, n, nu=cfg.nu, dt=dt, scheme=2)) as s:
         s.set_state(st.u, st.v, st.w, st.p)
-        s.step(3)
+        s.step(10)
         got = s.get_state()
         d = s.diag()
+    for k, r in (("u", ref.u), ("v", ref.v), ("w", ref.w), ("p", ref.p), ("hx", ref.px), ("hy", ref.py), ("hz", ref.pz)):
+        assert rel_l2(got[k], r) < 1e-10, k
+    assert d["max_div"] < 1e-12
+
+
+def test_wall_box_256x128x256_ten_steps_match_the_oracle():
+    """The wall-bounded configuration at its own size: FFT in x and z, the
+    wall-normal line solve in y (DCT_poisson_solver's operator,
+    NS_functions.f90:1505-1630), no-slip ADI rows (vel_bc_staggered_CN2)."""
+    import bench
+    from ns_3d_staggered_dp_gb300 import Session, make_config
+    nx, ny, nz = 256, 128, 256
+    cfg = O.Config(nx, ny, nz, lx=2 * np.pi, ly=2.0, lz=2 * np.pi, nu=1.0 / 180.0, dt=2e-3, scheme=O.AB2_CN,
+                   bc=(1, 2, 1), pbc=(1, 3, 1))
+    u, v, w, p = bench.channel_initial_field(nx, ny, nz)
+    O.vel_bc_staggered(u, v, w, O.Faces.zeros(nx, ny, nz), *cfg.bc)
+    st = O.State(u, v, w, p, np.zeros_like(u), np.zeros_like(v), np.zeros_like(w), first=True)
+    with Session(make_config(nx, ny, nz, lx=cfg.lx, ly=cfg.ly, lz=cfg.lz, nu=cfg.nu, dt=cfg.dt, scheme=2,
+                             bc=cfg.bc, pbc=cfg.pbc)) as s:
+        s.set_state(u, v, w, p)
+        s.step(10)
+        got = s.get_state()
+        d = s.diag()
+    ref = O.run(st, cfg, 10)
     for k, r in (("u", ref.u), ("v", ref.v), ("w", ref.w), ("p", ref.p), ("hx", ref.px), ("hy", ref.py), ("hz", ref.pz)):
         assert rel_l2(got[k], r) < 1e-10, k
     assert d["max_div"] < 1e-12

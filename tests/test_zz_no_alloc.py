@@ -1,6 +1,6 @@
 """ns_poisson_fft_noalloc: the FFT pressure Poisson solve for callers that
-must not allocate device memory (code under CUDA stream capture, hosts whose
-device memory belongs to another allocator, real-time loops).
+must not allocate device memory (hosts whose device memory belongs to
+another allocator or is reserved up front, real-time loops).
 
 Called through the C ABI with caller-owned device buffers, twice in a row per
 grid, and checked against the allocating entry point (ns_poisson) to the
@@ -65,3 +65,5 @@ def test_noalloc_rejects_grids_beyond_the_static_scratch():
     assert lib.ns_poisson_fft_noalloc(p, p, 128, 64, 64, 1.0, 1.0, 1.0, None) == 1    # NS_ERR_SHAPE
     assert lib.ns_poisson_fft_noalloc(p, p, 48, 32, 32, 1.0, 1.0, 1.0, None) == 1
     assert lib.ns_poisson_fft_noalloc(None, p, 32, 32, 32, 1.0, 1.0, 1.0, None) == 6  # NS_ERR_ARG
+    odd = ctypes.c_void_p(a.data_ptr() + 4)                                             # dp not 8-byte aligned
+    assert lib.ns_poisson_fft_noalloc(p, odd, 32, 32, 32, 1.0, 1.0, 1.0, None) == 6
