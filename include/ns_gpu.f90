@@ -120,6 +120,13 @@ module ns_gpu
       type(c_ptr), intent(in) :: faces(24)   ! c_loc of bx_u_1 ... bz_p_nz, or c_null_ptr
     end function
 
+    ! mean(dp_sub) of the DCT solve's singular mode (re_simulation_sub_tstep_interBC_combine.f90:766-768)
+    integer(c_int) function ns_set_mean_dp(h, mean_dp) bind(C, name="ns_set_mean_dp")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), value :: mean_dp
+    end function
+
     integer(c_int) function ns_step(h, nsteps) bind(C, name="ns_step")
       import :: c_int, c_ptr
       type(c_ptr), value :: h

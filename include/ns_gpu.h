@@ -143,8 +143,17 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
  * set == 0: the faces used by vel_bc_staggered and the pressure BC;
  * set == 1, 2, 3: the faces of the x, y, z AB2-CN sweep
  * (vel_bc_staggered_CN2, big_periodic_3D.f90:425,437,462).  A NULL entry
- * means zero.  Faces persist until set again. */
+ * means zero.  Faces persist until set again.  The copy is stream-ordered
+ * (the next ns_step sees the new faces) and the call returns without waiting
+ * for the device; the host arrays may be reused at once. */
 int ns_set_faces(ns_handle* h, int set, const double* const faces[24]);
+
+/* The mean imposed on the singular mode of a DCT/DST pressure solve from the
+ * next step on (the mean(dp_sub) argument of DCT_poisson_solver,
+ * re_simulation_sub_tstep_interBC_combine.f90:766-768, which a re-simulation
+ * driver changes every step).  Stream-ordered like ns_set_faces; boxes
+ * without a singular mode ignore it. */
+int ns_set_mean_dp(ns_handle* h, double mean_dp);
 
 /* Advance nsteps steps (the loop body of big_periodic_3D.f90:326-567). */
 int ns_step(ns_handle* h, int nsteps);

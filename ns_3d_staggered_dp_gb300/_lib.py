@@ -71,6 +71,7 @@ SIGNATURES = {
     "ns_get_state": (C.c_int, [C.c_void_p] + [_DP] * 7),
     "ns_set_faces": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(_DP)]),
     "ns_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "ns_set_mean_dp": (C.c_int, [C.c_void_p, C.c_double]),
     "ns_step_host": (C.c_int, [C.c_void_p] + [_DP] * 14),
     "ns_get_diag": (C.c_int, [C.c_void_p, C.POINTER(NSDiag)]),
     "ns_get_stage": (C.c_int, [C.c_void_p] + [_DP] * 4),

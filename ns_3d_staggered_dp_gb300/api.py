@@ -144,6 +144,10 @@ class Session:
                 arr[i] = None
         self._check(self.lib.ns_set_faces(self.h, which, arr))
 
+    def set_mean_dp(self, mean_dp):
+        """mean(dp_sub) of the DCT solve's singular mode from the next step on (ns_set_mean_dp)."""
+        self._check(self.lib.ns_set_mean_dp(self.h, float(mean_dp)))
+
     def step(self, n=1):
         self._check(self.lib.ns_step(self.h, n))
 

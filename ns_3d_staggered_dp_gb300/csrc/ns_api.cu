@@ -850,7 +850,12 @@ int build_plans(ns_handle* h) {
     double dense_other = 1.0;
     for (int a = 0; a < 3; ++a)
       if (a != sax && P.kind[a] == 1) dense_other *= n3[a];
-    P.mean_val = c.mean_dp * dense_other;  // mean of the singular line
+    // mean of the singular line: dense_other * mean_dp, mean_dp read on the
+    // device so that ns_set_mean_dp changes it without a new plan or graph
+    if (!h->mean_dev) NS_CUDA(h, cudaMalloc(&h->mean_dev, sizeof(double)));
+    NS_CUDA(h, cudaMemcpyAsync(h->mean_dev, &c.mean_dp, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    P.mean_val = dense_other;
+    P.mean_dev = h->mean_dev;
   } else if (allper && c.poisson_z == 0) {
     // cyclic z solve: the x and y eigenvalues give each z line's diagonal
     o_ex = tab.size();
@@ -962,6 +967,7 @@ void free_all(ns_handle* h) {
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (h->spec) cudaFree(h->spec);
+  if (h->mean_dev) cudaFree(h->mean_dev);
   if (h->cyc_buf) cudaFree(h->cyc_buf);
   if (h->stage) cudaFree(h->stage);
   if (h->stage2) cudaFree(h->stage2);
@@ -1381,24 +1387,42 @@ int ns_step_host(ns_handle* h, const double* u, const double* v, const double* w
 
 int ns_set_faces(ns_handle* h, int set, const double* const faces[24]) {
   if (!h || set < 0 || set > 3 || !faces) return fail(h, NS_ERR_ARG, "set must be 0..3");
-  // reference order: field-major (u, v, w, p), then x/y/z, then low/high
+  // The 24 planes of a set are contiguous in face_buf: repack them into one
+  // host buffer and send them with one stream-ordered copy (the copy from
+  // pageable memory is staged before the call returns, so the buffer can be
+  // reused).  Reference order: field-major (u, v, w, p), then x/y/z, then
+  // low/high.
+  const size_t base = face_offset(h->L, set, 0, 0, 0);
+  size_t n_set = 0;
+  for (int ax = 0; ax < 3; ++ax) n_set += 8 * plane_size(h->L, ax);
+  h->face_host.assign(n_set, 0.0);
   bool any = false;
   for (int fld = 0; fld < 4; ++fld)
     for (int ax = 0; ax < 3; ++ax)
       for (int side = 0; side < 2; ++side) {
         const double* src = faces[fld * 6 + ax * 2 + side];
-        const size_t n = plane_size(h->L, ax);
-        std::vector<double> plane(n, 0.0);
-        if (src) {
-          face_to_plane(h->cfg, h->L, ax, fld, src, plane.data());
-          any = true;
-        }
-        double* dst = h->face_buf + face_offset(h->L, set, ax, fld, side);
-        NS_CUDA(h, cudaMemcpyAsync(dst, plane.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        NS_CUDA(h, cudaStreamSynchronize(h->stream));
+        if (!src) continue;
+        face_to_plane(h->cfg, h->L, ax, fld, src, h->face_host.data() + (face_offset(h->L, set, ax, fld, side) - base));
+        any = true;
       }
+  NS_CUDA(h, cudaMemcpyAsync(h->face_buf + base, h->face_host.data(), n_set * sizeof(double), cudaMemcpyHostToDevice,
+                             h->stream));
+  // The captured step reads the faces from fixed device addresses; only a
+  // change between all-zero (null face arguments) and given faces needs a new graph.
+  if (h->face_set_nonzero[set] != any && h->graph) {
+    NS_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
   h->face_set_nonzero[set] = any;
-  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return NS_OK;
+}
+
+int ns_set_mean_dp(ns_handle* h, double mean_dp) {
+  if (!h) return NS_ERR_ARG;
+  h->cfg.mean_dp = mean_dp;
+  if (h->mean_dev)
+    NS_CUDA(h, cudaMemcpyAsync(h->mean_dev, &h->cfg.mean_dp, sizeof(double), cudaMemcpyHostToDevice, h->stream));
   return NS_OK;
 }
 

@@ -45,6 +45,8 @@ struct ns_handle {
   ns::LineSys sys[3][3];  // [axis][field]
   // faces: [set 0..3][axis][field 0..3][side] -> device planes
   double* face_buf = nullptr;
+  std::vector<double> face_host;  // host staging of one face set (ns_set_faces)
+  double* mean_dev = nullptr;     // mean_dp of the singular mode on the device (ns_set_mean_dp)
   ns::FaceSet faces[4]{};
   bool face_set_nonzero[4] = {false, false, false, false};
   unsigned long long* diag_bits = nullptr;

@@ -236,3 +236,40 @@ def test_batch_bench_set_of_64_boxes_matches_oracle():
         for k, rr in (("u", r.u), ("v", r.v), ("w", r.w), ("p", r.p)):
             err = rel_l2(g[k], rr)
             assert err < STEP_TOL, (i, subs[i], k, err)
+
+
+def test_plain_session_loop_matches_the_batch():
+    """The plain path of the re-simulation (one session per subdomain, faces
+    and mean dp set every step with ns_set_faces / ns_set_mean_dp, the graph
+    kept across face changes) follows the batch's result from the same start
+    and the same captured faces to 1e-10."""
+    from ns_3d_staggered_dp_gb300 import FACE_ORDER, Session, make_config
+    parent = _parent()
+    subs = P1_SUBS
+    with make_batch(subs, 8, restart=1) as b:
+        b.init_from_parent(parent)
+        for k in range(1, 7):
+            parent.step(1)
+            b.capture(parent, k, k * DT0)
+        b.advance(0.0)
+        init = [b.get_state(i) for i in range(len(subs))]
+        sess = []
+        for (x0, y0, z0, nx, ny, nz, _), st in zip(subs, init):
+            s = Session(make_config(nx, ny, nz, lx=nx * H, ly=ny * H, lz=nz * H, nu=NU, dt=DT0, scheme=1,
+                                    bc=(2, 2, 2), pbc=(3, 3, 3), dp_flag=1, gauge=0))
+            s.set_state(st["u"], st["v"], st["w"], st["p"], (st["hx"], st["hy"], st["hz"]))
+            sess.append(s)
+        for q in range(1, 5):
+            b.advance(q * DT0)
+            for i, s in enumerate(sess):
+                faces, mean = b.get_snapshot(q + 1, i)
+                s.set_faces({k: faces[k] for k in FACE_ORDER})
+                s.set_mean_dp(mean)
+                s.step(1)
+        for i, s in enumerate(sess):
+            a = s.get_state(history=False)
+            g = b.get_state(i, history=False)
+            for k in ("u", "v", "w", "p"):
+                assert rel_l2(a[k], g[k]) < STEP_TOL, (i, k, rel_l2(a[k], g[k]))
+            s.close()
+    parent.close()
