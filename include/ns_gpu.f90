@@ -24,7 +24,8 @@ module ns_gpu
     real(c_double) :: mean_dp
     integer(c_int) :: cn_periodic_closure, use_graph
     integer(c_int) :: poisson_z
-    integer(c_int) :: reserved(7)
+    integer(c_int) :: keep_sweeps   ! AB2-CN: keep u* after the x and y sweeps (per-sweep sub-block faces)
+    integer(c_int) :: reserved(6)
   end type ns_config
 
   type, bind(C) :: ns_diag
@@ -153,6 +154,13 @@ module ns_gpu
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: h
       real(c_double), intent(out), optional :: us(*), vs(*), ws(*), dp(*)
+    end function
+
+    ! u*, v*, w* after the x sweep and after the y sweep of the last AB2-CN step (cfg%keep_sweeps = 1)
+    integer(c_int) function ns_get_sweeps(h, ux, vx, wx, uy, vy, wy) bind(C, name="ns_get_sweeps")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out), optional :: ux(*), vx(*), wx(*), uy(*), vy(*), wy(*)
     end function
 
     ! TGV (NS_functions.f90:18-50) on the GPU: call ns_tgv(xu, nx+1, yu, ny+2, nz+2, t, nu, u=u) etc.
@@ -286,6 +294,21 @@ module ns_gpu
       integer(c_int), value :: slot, i
       type(c_ptr), intent(in) :: faces(24)         ! c_loc of the 24 output arrays, or c_null_ptr
       real(c_double), intent(out), optional :: mean_dp
+    end function
+
+    ! AB2-CN batches: the 18 per-sweep faces bx_u_1s ... bz_w_nzs (big_periodic_3D.f90:433-489)
+    integer(c_int) function ns_batch_set_sweep_faces(b, slot, i, faces) bind(C, name="ns_batch_set_sweep_faces")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b
+      integer(c_int), value :: slot, i
+      type(c_ptr), intent(in) :: faces(18)         ! c_loc of each array, or c_null_ptr (zero)
+    end function
+
+    integer(c_int) function ns_batch_get_sweep_faces(b, slot, i, faces) bind(C, name="ns_batch_get_sweep_faces")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b
+      integer(c_int), value :: slot, i
+      type(c_ptr), intent(in) :: faces(18)
     end function
 
     integer(c_int) function ns_batch_launch_count(b, launches) bind(C, name="ns_batch_launch_count")

@@ -76,7 +76,12 @@ typedef struct ns_config {
   int poisson_z;        /* all-periodic boxes, the z stage of the Poisson solve:
                            0: cyclic tridiagonal line solves (Sherman-Morrison),
                            1: z FFT, divide by the eigenvalue, z IFFT            */
-  int reserved[7];
+  int keep_sweeps;      /* AB2-CN: 1 keeps u*, v*, w* after the x and the y sweep
+                           of the last step readable (3 more fields): the
+                           per-sweep faces that a parent run records for its
+                           sub-blocks (big_periodic_3D.f90:433-489), read by
+                           ns_batch_capture and ns_get_sweeps                 */
+  int reserved[6];
 } ns_config;
 
 /* Diagnostics (big_periodic_3D.f90:572-579). */
@@ -168,6 +173,12 @@ int ns_get_diag(ns_handle* h, ns_diag* d);
  * for its sub-blocks (big_periodic_3D.f90:664-712).  Any pointer may be
  * NULL.  Valid after ns_step; a synchronous call. */
 int ns_get_stage(ns_handle* h, double* u_star, double* v_star, double* w_star, double* dp);
+
+/* u*, v*, w* of the last AB2-CN step after the x sweep (ux, vx, wx) and after
+ * the y sweep (uy, vy, wy), reference shapes, any pointer NULL to skip: the
+ * fields from which big_periodic_3D.f90:433-458 takes the per-sweep faces
+ * bx_?_1s ... by_?_nys.  Needs cfg.keep_sweeps = 1; a synchronous call. */
+int ns_get_sweeps(ns_handle* h, double* ux, double* vx, double* wx, double* uy, double* vy, double* wy);
 
 /* TGV (NS_functions.f90:18-50): the 2D Taylor-Green vortex at time t on the
  * tensor grid x(1:nx) x y(1:ny) x nz planes, computed on the GPU:
@@ -284,7 +295,10 @@ typedef struct ns_subdomain {
 } ns_subdomain;
 
 typedef struct ns_batch_config {
-  int scheme;           /* NS_EULER or NS_AB2 (sub_tstep > 1 needs NS_AB2)      */
+  int scheme;           /* NS_EULER, NS_AB2 or NS_AB2_CN (sub_tstep > 1 needs
+                           NS_AB2; NS_AB2_CN needs sub_tstep = 1, as the
+                           reference, :356-359, and the u* faces of every ADI
+                           sweep: a parent created with keep_sweeps = 1)      */
   int bc;               /* velocity bc of every subdomain face: 2 or 4           */
   int pbc;              /* pressure bc: 2, 3 or 4                                */
   int restart;          /* 1: AB2 from the first step with the parent's history  */
@@ -350,6 +364,17 @@ int ns_batch_set_snapshot(ns_batch* b, int slot, double t, int i, const double* 
  * boundary arrays the reference's parent run writes to its sub-block record
  * files (big_periodic_3D.f90:664-712). */
 int ns_batch_get_snapshot(ns_batch* b, int slot, int i, double* const faces[24], double* mean_dp);
+/* AB2-CN batches: the 18 per-sweep faces of snapshot slot `slot` of
+ * subdomain i, which the sub-block's x, y and z sweeps take as their BC rows
+ * (vel_bc_staggered_CN2, NS_functions.f90:313-410).  Order and shapes are the
+ * reference's records of big_periodic_3D.f90:433-489: bx_u_1s, bx_u_nxs,
+ * bx_v_1s, bx_v_nxs, bx_w_1s, bx_w_nxs, by_u_1s, ..., by_w_nys, bz_u_1s, ...,
+ * bz_w_nzs, each shaped as the get_velpr_bc face of the same name.
+ * ns_batch_capture fills them from the parent; _set (after the slot's
+ * ns_batch_set_snapshot; NULL entries zero) and _get move them to and from
+ * host arrays. */
+int ns_batch_set_sweep_faces(ns_batch* b, int slot, int i, const double* const faces[18]);
+int ns_batch_get_sweep_faces(ns_batch* b, int slot, int i, double* const faces[18]);
 
 /* Advance every subdomain over one parent interval [t0, t0 + dt0]: the
  * first call takes sub_tstep sub-steps, later calls one step. */
@@ -363,7 +388,8 @@ int ns_batch_autotune(ns_batch* b, int reps);
 /* Device time of every stage kernel of one regular step (mean over reps
  * launches, on a copy of the state), in the stage order interp, predict,
  * vel_bc x/y/z, x forward, y forward, z solve, y inverse, x inverse,
- * pr_bc x/y/z, correct, hist: ms_per_stage[16] (the last two unused). */
+ * pr_bc x/y/z, correct, hist: ms_per_stage[16] (the last two unused).  With
+ * AB2-CN the vel_bc x/y/z entries are the x, y, z ADI sweeps. */
 int ns_batch_profile(ns_batch* b, int reps, double* ms_per_stage);
 int ns_batch_get_config(const ns_batch* b, ns_batch_config* out);
 

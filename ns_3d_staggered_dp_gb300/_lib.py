@@ -28,7 +28,8 @@ class NSConfig(C.Structure):
         ("cn_periodic_closure", C.c_int),
         ("use_graph", C.c_int),
         ("poisson_z", C.c_int),
-        ("reserved", C.c_int * 7),
+        ("keep_sweeps", C.c_int),
+        ("reserved", C.c_int * 6),
     ]
 
 
@@ -75,6 +76,7 @@ SIGNATURES = {
     "ns_step_host": (C.c_int, [C.c_void_p] + [_DP] * 14),
     "ns_get_diag": (C.c_int, [C.c_void_p, C.POINTER(NSDiag)]),
     "ns_get_stage": (C.c_int, [C.c_void_p] + [_DP] * 4),
+    "ns_get_sweeps": (C.c_int, [C.c_void_p] + [_DP] * 6),
     "ns_tgv": (C.c_int, [_DP, C.c_int, _DP, C.c_int, C.c_int, C.c_double, C.c_double] + [_DP] * 4),
     "ns_cal_conv": (C.c_int, [C.c_void_p] + [_DP] * 6),
     "ns_cal_diff": (C.c_int, [C.c_void_p] + [_DP] * 6),
@@ -96,6 +98,8 @@ SIGNATURES = {
     "ns_batch_capture": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double]),
     "ns_batch_set_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(_DP), C.c_double]),
     "ns_batch_get_snapshot": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(_DP), _DP]),
+    "ns_batch_set_sweep_faces": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(_DP)]),
+    "ns_batch_get_sweep_faces": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(_DP)]),
     "ns_batch_advance": (C.c_int, [C.c_void_p, C.c_double]),
     "ns_batch_max_div": (C.c_int, [C.c_void_p, C.c_int, _DP]),
     "ns_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),

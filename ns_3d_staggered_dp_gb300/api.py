@@ -19,6 +19,12 @@ from . import _lib
 EULER, AB2, AB2_CN = 0, 1, 2
 PI = 3.1415926535897932
 
+SWEEP_FACE_ORDER = [  # per-sweep AB2-CN faces, as big_periodic_3D.f90:433-489 records them
+    "x_u_1", "x_u_n", "x_v_1", "x_v_n", "x_w_1", "x_w_n",
+    "y_u_1", "y_u_n", "y_v_1", "y_v_n", "y_w_1", "y_w_n",
+    "z_u_1", "z_u_n", "z_v_1", "z_v_n", "z_w_1", "z_w_n",
+]
+
 FACE_ORDER = [  # get_velpr_bc output order (NS_functions.f90:414-420)
     "x_u_1", "x_u_n", "y_u_1", "y_u_n", "z_u_1", "z_u_n",
     "x_v_1", "x_v_n", "y_v_1", "y_v_n", "z_v_1", "z_v_n",
@@ -175,6 +181,15 @@ class Session:
         self._check(self.lib.ns_get_diag(self.h, C.byref(d)))
         return {"max_div": d.max_div, "probe": d.probe, "steps": d.steps_done,
                 "euler_start_pending": bool(d.euler_start_pending)}
+
+    def get_sweeps(self):
+        """u*, v*, w* after the x sweep and after the y sweep of the last
+        AB2-CN step (keep_sweeps sessions; ns_get_sweeps)."""
+        sh = self.shapes
+        keys = ("ux", "vx", "wx", "uy", "vy", "wy")
+        out = {k: np.zeros(sh[k[0]], order="F") for k in keys}
+        self._check(self.lib.ns_get_sweeps(self.h, *[_ptr(out[k]) for k in keys]))
+        return out
 
     def get_stage(self):
         """u*, v*, w* and the gauge-shifted dp of the last step (ns_get_stage):
@@ -443,6 +458,22 @@ class Batch:
         m = C.c_double()
         self._check(self.lib.ns_batch_get_snapshot(self.h, int(slot), int(i), arr, C.byref(m)))
         return faces, m.value
+
+    def get_sweep_faces(self, slot, i):
+        """AB2-CN: {name: array} of the 18 per-sweep faces of snapshot slot
+        `slot` of subdomain i (SWEEP_FACE_ORDER names, ns_batch_get_sweep_faces)."""
+        _, _, _, nx, ny, nz, _ = self.subs[i]
+        fs = face_shapes(nx, ny, nz)
+        faces = {k: np.zeros(fs[k], order="F") for k in SWEEP_FACE_ORDER}
+        arr = (C.POINTER(C.c_double) * 18)(*[_ptr(faces[k]) for k in SWEEP_FACE_ORDER])
+        self._check(self.lib.ns_batch_get_sweep_faces(self.h, int(slot), int(i), arr))
+        return faces
+
+    def set_sweep_faces(self, slot, i, faces: dict):
+        """AB2-CN: the per-sweep faces of slot `slot` of subdomain i (missing = zero)."""
+        keep = [_f(faces[k]) if faces.get(k) is not None else None for k in SWEEP_FACE_ORDER]
+        arr = (C.POINTER(C.c_double) * 18)(*[_ptr(a) if a is not None else None for a in keep])
+        self._check(self.lib.ns_batch_set_sweep_faces(self.h, int(slot), int(i), arr))
 
     def advance(self, t0):
         self._check(self.lib.ns_batch_advance(self.h, float(t0)))

@@ -17,13 +17,6 @@ using namespace ns;
 
 namespace {
 
-// Host description of one tridiagonal line system of an ADI sweep.
-struct HostLineSys {
-  std::vector<double> l, dinv, cu, z;
-  double s0 = 0, s1 = 0;
-  int zA = 0, zB = 0, lo = 0, hi = 0, periodic = 0, n = 0;
-};
-
 // LU factors (no pivoting) of tridiag(a, b, c), a[0] and c[m-1] unused.
 void thomas_factor(const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& c,
                    HostLineSys& S) {
@@ -48,13 +41,16 @@ std::vector<double> thomas_solve(const HostLineSys& S, std::vector<double> r) {
   return r;
 }
 
+}  // namespace
+
+namespace ns {
 // CN system of one sweep axis (mat_CN, NS_functions.f90:1245-1294).
 // normal: the swept field is staggered along the axis (A matrix, n+1
 // unknowns); otherwise tangential (B matrix, n+2 unknowns).
 // transposed (periodic only): the system M^T of the adjoint sweep, whose
 // corner entries are those of M exchanged.
 HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool normal, int closure,
-                            bool transposed = false) {
+                            bool transposed) {
   const double idx2 = 1.0 / (h * h);
   const double dg = 1.0 + 0.5 * dt * nu * 2.0 * idx2;
   const double of = -0.5 * dt * nu * 1.0 * idx2;
@@ -118,9 +114,7 @@ HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool 
   S.z.assign(1, 0.0);
   return S;
 }
-
-
-}  // namespace
+}  // namespace ns
 
 namespace ns {
 
@@ -439,6 +433,7 @@ int validate(const ns_config& c, std::string& msg) {
   if (c.nx < 4 || c.ny < 4 || c.nz < 4) { msg = "grid too small"; return NS_ERR_SHAPE; }
   if (c.scheme < 0 || c.scheme > 2) { msg = "scheme must be 0 (Euler), 1 (AB2) or 2 (AB2-CN)"; return NS_ERR_ARG; }
   if (c.poisson_z != 0 && c.poisson_z != 1) { msg = "poisson_z must be 0 (cyclic line solves) or 1 (z FFT)"; return NS_ERR_ARG; }
+  if (c.keep_sweeps != 0 && c.keep_sweeps != 1) { msg = "keep_sweeps must be 0 or 1"; return NS_ERR_ARG; }
   for (int a = 0; a < 3; ++a) {
     if (c.bc[a] != 1 && c.bc[a] != 2 && c.bc[a] != 4) {
       msg = "velocity bc must be 1, 2 or 4 (3 leaves the ghosts undefined in the reference)";
@@ -562,14 +557,17 @@ namespace {
 // The three sweeps with fixed buffer roles: x reads A (the predictor's
 // output) and writes B, y reads B and writes A, z reads A and writes B, so
 // the final u*, v*, w* are in B on every step (and in every captured graph).
+// With keep_sweeps the x sweep writes C instead (and y reads C), so after a
+// step C holds u* after the x sweep, A after the y sweep, B after the z sweep.
 AdiArgs adi_args(ns_handle* h, int ax) {
   double* A[3] = {h->us, h->vs, h->ws};
   double* B[3] = {h->us2, h->vs2, h->ws2};
+  double* X[3] = {h->us3 ? h->us3 : h->us2, h->vs3 ? h->vs3 : h->vs2, h->ws3 ? h->ws3 : h->ws2};
   AdiArgs a{};
   a.L = h->L;
   for (int f = 0; f < 3; ++f) {
-    a.src[f] = (ax == 1) ? B[f] : A[f];
-    a.dst[f] = (ax == 1) ? A[f] : B[f];
+    a.src[f] = (ax == 1) ? X[f] : A[f];
+    a.dst[f] = (ax == 1) ? A[f] : (ax == 0 ? X[f] : B[f]);
     a.sys[f] = h->sys[ax][f];
     a.face_lo[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][0] : nullptr;
     a.face_hi[f] = h->face_set_nonzero[1 + ax] ? h->faces[1 + ax].ax[ax].f[f][1] : nullptr;
@@ -963,7 +961,7 @@ void free_all(ns_handle* h) {
   ns::api_free_adjoint(h);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   double* bufs[] = {h->u, h->v, h->w, h->p, h->hx, h->hy, h->hz, h->us, h->vs, h->ws, h->dp, h->inv_lam, h->adi_buf, h->face_buf,
-                    h->us2, h->vs2, h->ws2};
+                    h->us2, h->vs2, h->ws2, h->us3, h->vs3, h->ws3};
   for (double* b : bufs)
     if (b) cudaFree(b);
   if (h->spec) cudaFree(h->spec);
@@ -1066,6 +1064,13 @@ int ns_create(const ns_config* cfg, ns_handle** out) {
   for (double** f : fields) {
     if (cudaMalloc(f, h->L.fsize * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
     if (cudaMemsetAsync(*f, 0, h->L.fsize * sizeof(double), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+  }
+  if (cfg->keep_sweeps && cfg->scheme == NS_AB2_CN) {
+    double** kept[] = {&h->us3, &h->vs3, &h->ws3};
+    for (double** f : kept) {
+      if (cudaMalloc(f, h->L.fsize * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+      if (cudaMemsetAsync(*f, 0, h->L.fsize * sizeof(double), h->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+    }
   }
   const size_t ft = face_total(h->L);
   if (cudaMalloc(&h->face_buf, ft * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
@@ -1572,6 +1577,18 @@ int ns_get_stage(ns_handle* h, double* us, double* vs, double* ws, double* dp) {
     }
     NS_CUDA(h, cudaMemcpyAsync(dp, h->stage, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   }
+  NS_CUDA(h, cudaStreamSynchronize(h->stream));
+  return NS_OK;
+}
+
+int ns_get_sweeps(ns_handle* h, double* ux, double* vx, double* wx, double* uy, double* vy, double* wy) {
+  if (!h) return NS_ERR_ARG;
+  if (!h->us3) return fail(h, NS_ERR_ARG, "ns_get_sweeps needs an AB2-CN session created with keep_sweeps = 1");
+  if (h->steps == 0) return fail(h, NS_ERR_ARG, "no step taken since ns_set_state");
+  double* const dst[6] = {ux, vx, wx, uy, vy, wy};
+  const double* src[6] = {h->us3, h->vs3, h->ws3, h->us, h->vs, h->ws};
+  for (int q = 0; q < 6; ++q)
+    if (dst[q]) NS_CUDA(h, d2h_field(h, dst[q], src[q], q % 3));
   NS_CUDA(h, cudaStreamSynchronize(h->stream));
   return NS_OK;
 }

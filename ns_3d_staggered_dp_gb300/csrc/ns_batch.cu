@@ -108,13 +108,20 @@ __global__ void __launch_bounds__(kChunk) interp_kernel(const SubGeo* __restrict
 // the slot minus the field's slot offset on that axis.  Every value is formed
 // with the reference's operations in its order (no contraction into FMAs), so
 // the faces equal get_velpr_bc of the same arrays bit for bit.
+// With AB2-CN the buffer continues with the per-sweep planes: sweep a's
+// faces of u, v, w on axis a from the parent's u* after that sweep
+// (sw.f[a][field]), as big_periodic_3D.f90:433-489 records them.
+struct SweepSrc {
+  const double* f[3][3];
+};
 __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restrict__ geo,
                                                          const BatchItem* __restrict__ items, int n_items, Layout Lp,
                                                          const double* __restrict__ pus, const double* __restrict__ pvs,
                                                          const double* __restrict__ pws, const double* __restrict__ pdp,
                                                          const double* __restrict__ pprev, double dt,
                                                          double* __restrict__ slot_base, int bc, int pbc, double dx,
-                                                         double dy, double dz, const double* __restrict__ gauge) {
+                                                         double dy, double dz, const double* __restrict__ gauge,
+                                                         SweepSrc sw) {
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const BatchItem w = items[it];
     const SubGeo& g = geo[w.sub];
@@ -123,6 +130,7 @@ __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restric
     double* out = slot_base + g.snap_off + e;
     const Layout& L = g.L;
     int a = 0, f = 0, side = 0;
+    bool sweep = false;
     {
       long long r = e;
       bool found = false;
@@ -130,6 +138,13 @@ __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restric
         const long long ps = (long long)plane_n1(L, aa) * plane_n2(L, aa);
         for (int q = 0; q < 8; ++q) {
           if (r < ps) { a = aa; f = q / 2; side = q % 2; found = true; break; }
+          r -= ps;
+        }
+      }
+      for (int aa = 0; aa < 3 && !found; ++aa) {  // the per-sweep planes
+        const long long ps = (long long)plane_n1(L, aa) * plane_n2(L, aa);
+        for (int q = 0; q < 6; ++q) {
+          if (r < ps) { a = aa; f = q / 2; side = q % 2; found = true; sweep = true; break; }
           r -= ps;
         }
       }
@@ -161,7 +176,7 @@ __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restric
         i0 = side ? na + 1 : 0; op = 0;
       }
     }
-    const double* F = f == 0 ? pus : (f == 1 ? pvs : (f == 2 ? pws : pdp));
+    const double* F = sweep ? sw.f[a][f] : (f == 0 ? pus : (f == 1 ? pvs : (f == 2 ? pws : pdp)));
     const int x0[3] = {g.x0, g.y0, g.z0};
     // parent slot along axis b of the 0-based sub-array index i: x0 + i - (face axis ? 0 : 1)
     int ia[3], ib[3];
@@ -178,7 +193,7 @@ __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restric
     const double g0 = (f == 3 && gauge) ? *gauge : 0.0;
     // u_bc_corr = u_bc + diff(p_previous)/h*dt on the velocity fields (u branch, dp_flag = 0):
     // diff(p) at the face slot s of field f is p[s] - p[s - e_f] in the slot layout
-    const bool corr = pprev && f < 3;
+    const bool corr = pprev && f < 3 && !sweep;
     const double hf = f == 0 ? dx : (f == 1 ? dy : dz);
     const long long ef = f == 0 ? 1 : (f == 1 ? Lp.sy : Lp.sz);
     auto val = [&](const int* s) {
@@ -345,6 +360,7 @@ struct ns_batch {
   double* arena = nullptr;       // fields of all subdomains
   size_t arena_n = 0;
   double* tables = nullptr;      // dense matrices and eigenvalues per size class
+  double* adi_tab = nullptr;     // AB2-CN: line-system factors per (axis, size, normal/tangential)
   double2* tri_tab = nullptr;    // z-solve multipliers of every subdomain (one per spectrum entry)
   double* snaps = nullptr;       // n_slots x (all faces)
   double* snap_mean = nullptr;   // n_slots x n
@@ -367,6 +383,7 @@ struct ns_batch {
   BatchSpecArgs* d_spec[2] = {nullptr, nullptr};
   CorrectArgs* d_corr[2] = {nullptr, nullptr};
   BatchBcArgs* d_bc = nullptr;
+  BatchAdiArgs* d_adi = nullptr;  // AB2-CN only
   // work items: per active set (0 regular, s >= 1 sub-step s of the first
   // interval), per stage: offset, count, and per-subdomain ranges
   BatchItem* d_items = nullptr;
@@ -400,10 +417,18 @@ int bfail(ns_batch* b, int code, const std::string& m) {
     if (e_ != cudaSuccess) return bfail((b), NS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-long long face_doubles(const Layout& L) {
+// A subdomain's face buffer: the 24 planes of get_velpr_bc ([axis][field
+// 0..3][side]), then with AB2-CN the 18 per-sweep planes ([sweep axis][field
+// 0..2][side], each over the other two axes).
+long long face_doubles(const Layout& L, bool cn = false) {
   long long t = 0;
-  for (int a = 0; a < 3; ++a) t += 8LL * plane_n1(L, a) * plane_n2(L, a);
+  for (int a = 0; a < 3; ++a) t += (cn ? 14LL : 8LL) * plane_n1(L, a) * plane_n2(L, a);
   return t;
+}
+long long sweep_face_off(const Layout& L, int a, int f, int side) {
+  long long o = face_doubles(L);
+  for (int q = 0; q < a; ++q) o += 6LL * plane_n1(L, q) * plane_n2(L, q);
+  return o + (long long)(2 * f + side) * plane_n1(L, a) * plane_n2(L, a);
 }
 
 // Launch the kernel(s) of one stage for active set `set` (one launch, or one
@@ -438,8 +463,9 @@ cudaError_t launch_stage_kernel(ns_batch* b, int set, int stage, bool first, cud
         hist_kernel<<<grid, kChunk, 0, st>>>(b->d_geo, p, cnt);
         e = cudaGetLastError();
         break;
-      case ST_VBC_X: case ST_VBC_Y: case ST_VBC_Z:
-        e = launch_bc_batch(stage - ST_VBC_X, false, b->d_bc, p, cnt, grid, st);
+      case ST_VBC_X: case ST_VBC_Y: case ST_VBC_Z:  // AB2-CN: the ADI sweeps take these slots
+        if (c.scheme == NS_AB2_CN) e = launch_adi_batch(stage - ST_VBC_X, b->d_adi, p, cnt, grid, st);
+        else e = launch_bc_batch(stage - ST_VBC_X, false, b->d_bc, p, cnt, grid, st);
         break;
       case ST_PBC_X: case ST_PBC_Y: case ST_PBC_Z:
         e = launch_bc_batch(stage - ST_PBC_X, true, b->d_bc, p, cnt, grid, st);
@@ -577,6 +603,7 @@ int ns_batch_destroy(ns_batch* b) {
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   if (b->arena) cudaFree(b->arena);
   if (b->tables) cudaFree(b->tables);
+  if (b->adi_tab) cudaFree(b->adi_tab);
   if (b->tri_tab) cudaFree(b->tri_tab);
   if (b->snaps) cudaFree(b->snaps);
   if (b->snap_mean) cudaFree(b->snap_mean);
@@ -598,7 +625,9 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   *out = nullptr;
   const ns_batch_config& c = *cfg;
   std::string msg;
-  if (c.scheme != NS_EULER && c.scheme != NS_AB2) msg = "batched scheme must be Euler or AB2";
+  if (c.scheme != NS_EULER && c.scheme != NS_AB2 && c.scheme != NS_AB2_CN) msg = "batched scheme must be Euler, AB2 or AB2-CN";
+  else if (c.scheme == NS_AB2_CN && !c.using_ustar)
+    msg = "AB2-CN re-simulation takes the parent's u* faces of every sweep (using_ustar = 1)";
   else if (c.bc != 2 && c.bc != 4) msg = "batched velocity bc must be 2 or 4";
   else if (c.pbc < 2 || c.pbc > 4) msg = "batched pressure bc must be 2, 3 or 4";
   else if (c.n_slots < 1) msg = "n_slots must be >= 1";
@@ -610,7 +639,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     if (d.nx < 4 || d.ny < 4 || d.nz < 4 || d.nx % 2 || d.nx > 1024 || d.ny > 128 || d.nz > 256)
       msg = "subdomain sizes: nx even <= 1024, ny <= 128, nz <= 256, all >= 4";
     else if (d.sub_tstep < 1 || (d.sub_tstep > 1 && c.scheme != NS_AB2))
-      msg = "sub_tstep >= 1 (> 1 only with AB2, re_simulation_sub_tstep_interBC_combine.f90:357-359)";
+      msg = "sub_tstep >= 1 (> 1 only with AB2, re_simulation_sub_tstep_interBC_combine.f90:356-359)";
     else if (d.x0 < 1 || d.y0 < 1 || d.z0 < 1) msg = "subdomain origins are 1-based";
     else if (!c.using_ustar && d.sub_tstep != 1)
       msg = "sub_tstep > 1 needs u* boundary values (re_simulation_sub_tstep_interBC_combine.f90:360-363)";
@@ -647,7 +676,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     const size_t fs = align32(b->L[i].fsize);
     tot += 14 * fs;                                                  // 11 fields + saved history
     tot += align32((size_t)(d.nx / 2) * d.ny * d.nz * 2);           // packed spectrum
-    tot += align32((size_t)face_doubles(b->L[i]));                   // current faces
+    tot += align32((size_t)face_doubles(b->L[i], c.scheme == NS_AB2_CN));  // current faces
     tot += 32;                                                       // mean dp
   }
   b->arena_n = tot;
@@ -666,7 +695,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     for (int f = 0; f < 3; ++f) g.save[f] = p + (11 + f) * fs;
     double* face = p + 14 * fs + align32((size_t)(L.nx / 2) * L.ny * L.nz * 2);
     g.face = face;
-    g.face_n = face_doubles(L);
+    g.face_n = face_doubles(L, c.scheme == NS_AB2_CN);
     g.mean = face + align32((size_t)g.face_n);
     g.snap_off = snap_tot;
     snap_tot += (long long)align32((size_t)g.face_n);
@@ -731,6 +760,46 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   // ---- per-subdomain plans and argument tables ----
   const double hs[3] = {c.dx, c.dy, c.dz};
   const int bc3[3] = {c.bc, c.bc, c.bc};
+  // AB2-CN: the factors of mat_CN_tridiagonal (NS_functions.f90:1296-1342) per
+  // (sweep axis, cells along it, normal / tangential), shared by the
+  // subdomains of the same size; sub_tstep is 1, so every step uses dt0.
+  const bool cn = c.scheme == NS_AB2_CN;
+  std::map<long long, LineSys> line_sys;
+  if (cn) {
+    constexpr int pad = 8;
+    std::vector<HostLineSys> hsys;
+    std::vector<long long> keys;
+    for (int i = 0; i < n; ++i) {
+      const int n3[3] = {subs[i].nx, subs[i].ny, subs[i].nz};
+      for (int a = 0; a < 3; ++a)
+        for (int normal = 0; normal < 2; ++normal) {
+          const long long key = ((long long)a * 4096 + n3[a]) * 2 + normal;
+          if (line_sys.count(key)) continue;
+          line_sys[key] = LineSys{};
+          keys.push_back(key);
+          hsys.push_back(build_cn_system(n3[a], c.bc, hs[a], c.dt0, c.nu, normal != 0, 0));
+        }
+    }
+    size_t total = 0;
+    for (const HostLineSys& S : hsys) total += 3 * (S.l.size() + 2 * pad);
+    std::vector<double> host(std::max<size_t>(total, 1), 0.0);
+    if (cudaMalloc(&b->adi_tab, host.size() * sizeof(double)) != cudaSuccess) return bail(NS_ERR_NOMEM);
+    size_t off = 0;
+    for (size_t q = 0; q < hsys.size(); ++q) {
+      const HostLineSys& S = hsys[q];
+      LineSys& D = line_sys[keys[q]];
+      const size_t m = S.l.size(), mp = m + 2 * pad;
+      std::memcpy(&host[off + pad], S.l.data(), m * sizeof(double)); D.l = b->adi_tab + off; off += mp;
+      std::memcpy(&host[off + pad], S.dinv.data(), m * sizeof(double)); D.dinv = b->adi_tab + off; off += mp;
+      std::memcpy(&host[off + pad], S.cu.data(), m * sizeof(double)); D.cu = b->adi_tab + off; off += mp;
+      D.z = nullptr; D.s0 = D.s1 = 0.0; D.zA = D.zB = 0;
+      D.lo = S.lo; D.hi = S.hi; D.periodic = 0; D.n = S.n; D.pad = pad;
+    }
+    if (cudaMemcpyAsync(b->adi_tab, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream) !=
+        cudaSuccess)
+      return bail(NS_ERR_CUDA);
+  }
+  std::vector<BatchAdiArgs> adia(cn ? n : 0);
   std::vector<PredictArgs> pred[2];
   std::vector<BatchSpecArgs> spec[2];
   std::vector<CorrectArgs> corr[2];
@@ -810,6 +879,19 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     ba = BatchBcArgs{};
     ba.L = L; ba.us = us; ba.vs = vs; ba.ws = ws; ba.dp = dp; ba.F = F;
     for (int a = 0; a < 3; ++a) { ba.bc[a] = c.bc; ba.pbc[a] = c.pbc; ba.h[a] = hs[a]; }
+    if (cn) {
+      BatchAdiArgs& aa = adia[i];
+      aa = BatchAdiArgs{};
+      aa.L = L;
+      aa.f[0] = us; aa.f[1] = vs; aa.f[2] = ws;
+      const int n3[3] = {d.nx, d.ny, d.nz};
+      for (int a = 0; a < 3; ++a)
+        for (int f = 0; f < 3; ++f) {
+          aa.sys[a][f] = line_sys[((long long)a * 4096 + n3[a]) * 2 + (f == a ? 1 : 0)];
+          aa.face_lo[a][f] = g.face + sweep_face_off(L, a, f, 0);
+          aa.face_hi[a][f] = g.face + sweep_face_off(L, a, f, 1);
+        }
+    }
   }
   for (int pass = 0; pass < 5; ++pass)
     for (int i = 0; i < n; ++i) b->spec_smem[pass] = std::max(b->spec_smem[pass], spec_pass_smem(pass, b->plan[i]));
@@ -830,7 +912,15 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
             for (int x = 0; x < gx; ++x) v.push_back(BatchItem{i, x, y, z});
         break;
       }
-      case ST_VBC_X: case ST_VBC_Y: case ST_VBC_Z: add1(chunks(plane_count(L, stage - ST_VBC_X)), 0); break;
+      case ST_VBC_X: case ST_VBC_Y: case ST_VBC_Z:
+        if (c.scheme == NS_AB2_CN) {  // the ADI sweep: 128-line chunks of each field
+          const int nl = plane_count(L, stage - ST_VBC_X);
+          for (int f = 0; f < 3; ++f)
+            for (int q = 0; q < (nl + kAdiBatchLines - 1) / kAdiBatchLines; ++q) v.push_back(BatchItem{i, q, f, 0});
+        } else {
+          add1(chunks(plane_count(L, stage - ST_VBC_X)), 0);
+        }
+        break;
       case ST_PBC_X: case ST_PBC_Y: case ST_PBC_Z: add1(chunks(plane_count(L, stage - ST_PBC_X)), 0); break;
       case ST_XF: case ST_YF: case ST_TRI: case ST_YI: case ST_XI: {
         const int pass_of[5] = {0, 2, 4, 3, 1};
@@ -891,6 +981,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   const size_t o_spec = o; o = al(o + 2 * n * sizeof(BatchSpecArgs));
   const size_t o_corr = o; o = al(o + 2 * n * sizeof(CorrectArgs));
   const size_t o_bc = o; o = al(o + n * sizeof(BatchBcArgs));
+  const size_t o_adi = o; o = al(o + adia.size() * sizeof(BatchAdiArgs));
   const size_t o_items = o; o = al(o + all.size() * sizeof(BatchItem));
   std::vector<unsigned char> hbuf(o, 0);
   std::memcpy(hbuf.data() + o_geo, b->geo.data(), n * sizeof(SubGeo));
@@ -900,6 +991,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     std::memcpy(hbuf.data() + o_corr + v * n * sizeof(CorrectArgs), corr[v].data(), n * sizeof(CorrectArgs));
   }
   std::memcpy(hbuf.data() + o_bc, bca.data(), n * sizeof(BatchBcArgs));
+  if (!adia.empty()) std::memcpy(hbuf.data() + o_adi, adia.data(), adia.size() * sizeof(BatchAdiArgs));
   std::memcpy(hbuf.data() + o_items, all.data(), all.size() * sizeof(BatchItem));
   if (cudaMalloc(&b->dev_args, o) != cudaSuccess) return bail(NS_ERR_NOMEM);
   if (cudaMemcpyAsync(b->dev_args, hbuf.data(), o, cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
@@ -911,6 +1003,7 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     b->d_corr[v] = reinterpret_cast<CorrectArgs*>(b->dev_args + o_corr) + v * n;
   }
   b->d_bc = reinterpret_cast<BatchBcArgs*>(b->dev_args + o_bc);
+  b->d_adi = adia.empty() ? nullptr : reinterpret_cast<BatchAdiArgs*>(b->dev_args + o_adi);
   b->d_items = reinterpret_cast<BatchItem*>(b->dev_args + o_items);
   // interpolation weights: one region per active set
   const size_t nw = (size_t)nsets * n * 6;
@@ -1009,6 +1102,16 @@ int ns_batch_capture(ns_batch* b, const ns_handle* parent, int slot, double t) {
   const double* psrc = c.dp_flag ? parent->dp : parent->p;
   const double* gauge = (c.dp_flag && parent->cfg.gauge) ? parent->dp + Lp.at(0, 0, 0) : nullptr;
   const bool corr = !c.using_ustar && !c.dp_flag;
+  SweepSrc sw{};
+  if (c.scheme == NS_AB2_CN) {  // u* after the x sweep (kept), after the y sweep (A), after the z sweep (B)
+    if (!cn || !parent->us3)
+      return bfail(b, NS_ERR_ARG, "an AB2-CN batch captures from an AB2-CN parent created with keep_sweeps = 1");
+    const double* after[3][3] = {{parent->us3, parent->vs3, parent->ws3},
+                                 {parent->us, parent->vs, parent->ws},
+                                 {parent->us2, parent->vs2, parent->ws2}};
+    for (int a = 0; a < 3; ++a)
+      for (int f = 0; f < 3; ++f) sw.f[a][f] = after[a][f];
+  }
   if (corr && b->p_prev_n != Lp.fsize) {  // first capture from this parent: p_prev = the current p
     if (b->p_prev) cudaFree(b->p_prev);
     b->p_prev = nullptr;
@@ -1026,7 +1129,7 @@ int ns_batch_capture(ns_batch* b, const ns_handle* parent, int slot, double t) {
   const ns_batch::Range& r = b->capture_rng;
   capture_kernel<<<persistent_grid(0, r.cnt), kChunk, 0, b->stream>>>(
       b->d_geo, b->d_items + r.off, r.cnt, Lp, pus, pvs, pws, psrc, corr ? b->p_prev : nullptr, c.dt0,
-      b->snaps + (size_t)slot * b->slot_stride, c.bc, c.pbc, c.dx, c.dy, c.dz, gauge);
+      b->snaps + (size_t)slot * b->slot_stride, c.bc, c.pbc, c.dx, c.dy, c.dz, gauge, sw);
   capture_mean_kernel<<<std::min(b->n, 1024), 256, 0, b->stream>>>(b->d_geo, b->n, Lp, psrc,
                                                                    b->snap_mean + (size_t)slot * b->n, gauge);
   if (corr) {  // this capture's p is the next capture's p_previous
@@ -1069,8 +1172,9 @@ int ns_batch_set_snapshot(ns_batch* b, int slot, double t, int i, const double* 
     for (int q = 0; q < e2; ++q)
       for (int r = 0; r < e1; ++r) plane[(size_t)(r + o1) + (size_t)n1 * (q + o2)] = src[r + (size_t)e1 * q];
   }
-  NB_CUDA(b, cudaMemcpyAsync(b->snaps + (size_t)slot * b->slot_stride + g.snap_off, buf.data(), buf.size() * sizeof(double),
-                             cudaMemcpyHostToDevice, b->stream));
+  // the get_velpr_bc planes only: an AB2-CN batch's per-sweep planes are set apart
+  NB_CUDA(b, cudaMemcpyAsync(b->snaps + (size_t)slot * b->slot_stride + g.snap_off, buf.data(),
+                             (size_t)face_doubles(L) * sizeof(double), cudaMemcpyHostToDevice, b->stream));
   NB_CUDA(b, cudaMemcpyAsync(b->snap_mean + (size_t)slot * b->n + i, &mean_dp, sizeof(double), cudaMemcpyHostToDevice,
                              b->stream));
   NB_CUDA(b, cudaStreamSynchronize(b->stream));
@@ -1112,6 +1216,53 @@ int ns_batch_get_snapshot(ns_batch* b, int slot, int i, double* const faces[24],
   }
   if (mean_dp) *mean_dp = m;
   return NS_OK;
+}
+
+// The per-sweep faces of an AB2-CN batch in the reference's order
+// (bx_u_1s, bx_u_nxs, bx_v_1s, bx_v_nxs, bx_w_1s, bx_w_nxs, by_u_1s, ..., bz_w_nzs),
+// each in the shape of the get_velpr_bc face of the same name.
+static int sweep_faces_copy(ns_batch* b, int slot, int i, double* const* out, const double* const* in) {
+  if (!b || slot < 0 || slot >= b->cfg.n_slots || i < 0 || i >= b->n) return NS_ERR_ARG;
+  if (b->cfg.scheme != NS_AB2_CN) return bfail(b, NS_ERR_ARG, "per-sweep faces belong to an AB2-CN batch");
+  const SubGeo& g = b->geo[i];
+  const Layout& L = g.L;
+  const long long off0 = face_doubles(L);
+  std::vector<double> buf((size_t)(g.face_n - off0), 0.0);
+  double* dev = b->snaps + (size_t)slot * b->slot_stride + g.snap_off + off0;
+  if (out) {
+    if (!b->snap_ok[slot]) return bfail(b, NS_ERR_ARG, "snapshot slot " + std::to_string(slot) + " is empty");
+    NB_CUDA(b, cudaMemcpyAsync(buf.data(), dev, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    NB_CUDA(b, cudaStreamSynchronize(b->stream));
+  }
+  for (int k = 0; k < 18; ++k) {
+    const int a = k / 6, f = (k % 6) / 2, s = k % 2;
+    const int a1 = a == 0 ? 1 : 0, a2 = a == 2 ? 1 : 2;
+    const int e1 = field_ext(L, f, a1), e2 = field_ext(L, f, a2);
+    const int o1 = f == a1 ? 1 : 0, o2 = f == a2 ? 1 : 0;
+    const int n1 = plane_n1(L, a);
+    double* plane = buf.data() + (sweep_face_off(L, a, f, s) - off0);
+    for (int q = 0; q < e2; ++q)
+      for (int r = 0; r < e1; ++r) {
+        const size_t pi = (size_t)(r + o1) + (size_t)n1 * (q + o2), hi = r + (size_t)e1 * q;
+        if (out && out[k]) out[k][hi] = plane[pi];
+        if (in && in[k]) plane[pi] = in[k][hi];
+      }
+  }
+  if (in) {
+    NB_CUDA(b, cudaMemcpyAsync(dev, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    NB_CUDA(b, cudaStreamSynchronize(b->stream));
+  }
+  return NS_OK;
+}
+
+int ns_batch_set_sweep_faces(ns_batch* b, int slot, int i, const double* const faces[18]) {
+  if (!faces) return NS_ERR_ARG;
+  return sweep_faces_copy(b, slot, i, nullptr, faces);
+}
+
+int ns_batch_get_sweep_faces(ns_batch* b, int slot, int i, double* const faces[18]) {
+  if (!faces) return NS_ERR_ARG;
+  return sweep_faces_copy(b, slot, i, faces, nullptr);
 }
 
 int ns_batch_advance(ns_batch* b, double t0) {

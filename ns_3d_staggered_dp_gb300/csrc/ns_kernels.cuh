@@ -187,6 +187,19 @@ struct AdiArgs {
   int z0, z1;                // x and y sweeps: only the lines of z slots [z0, z1) (z1 = 0: all)
 };
 cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st);
+// One subdomain of the batched AB2-CN sweeps (ns_batch.cu): u*, v*, w* swept
+// in place (walls only), the nine line systems and the BC-row planes of each
+// sweep (the parent's per-sweep faces, big_periodic_3D.f90:433-489).
+struct BatchAdiArgs {
+  Layout L;
+  double* f[3];                 // u*, v*, w*
+  LineSys sys[3][3];            // [axis][field]
+  const double* face_lo[3][3];  // [axis][field]: plane (other two axes, ghosts included) of the low BC row
+  const double* face_hi[3][3];
+};
+constexpr int kAdiBatchLines = 128;  // lines per work item (bx) of one field (by) of one subdomain
+cudaError_t launch_adi_batch(int axis, const BatchAdiArgs* tab, const BatchItem* items, int n_items, int grid,
+                             cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Periodic FFT Poisson (ns_fft.cu)

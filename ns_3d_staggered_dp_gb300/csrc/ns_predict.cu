@@ -550,6 +550,7 @@ cudaError_t launch_predict_batch(const PredictArgs* tab, const BatchItem* items,
   if (scheme == S && first == F && dpf == D) return launch_bt<S, F, D>(tab, items, n_items, grid, st);
   NS_PRED_CASE(0, false, false) NS_PRED_CASE(0, false, true) NS_PRED_CASE(0, true, false) NS_PRED_CASE(0, true, true)
   NS_PRED_CASE(1, false, false) NS_PRED_CASE(1, false, true) NS_PRED_CASE(1, true, false) NS_PRED_CASE(1, true, true)
+  NS_PRED_CASE(2, false, false) NS_PRED_CASE(2, false, true) NS_PRED_CASE(2, true, false) NS_PRED_CASE(2, true, true)
 #undef NS_PRED_CASE
   return cudaErrorInvalidValue;
 }

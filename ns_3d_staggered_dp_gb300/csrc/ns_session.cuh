@@ -25,6 +25,7 @@ struct ns_handle {
   double *hx = nullptr, *hy = nullptr, *hz = nullptr;
   double *us = nullptr, *vs = nullptr, *ws = nullptr, *dp = nullptr;
   double *us2 = nullptr, *vs2 = nullptr, *ws2 = nullptr;  // ADI ping-pong buffers
+  double *us3 = nullptr, *vs3 = nullptr, *ws3 = nullptr;  // x-sweep output (cfg.keep_sweeps only)
   double2* spec = nullptr;
   double* stage = nullptr;   // host<->device staging of one reference-shaped field
   double* stage2 = nullptr;  // second staging buffer (multi-field transfers)
@@ -93,4 +94,17 @@ void dense_pair(int n, int pb, std::vector<double>& F, std::vector<double>& G);
 double axis_eig(int n, int pb, int m, double h);
 // Predictor coefficients of a box with velocity codes bc (ns_api.cu).
 void set_predict_coeffs(PredictArgs& a, const int bc[3], double dx, double dy, double dz, double dt, double nu);
+// Host description of one tridiagonal line system of an ADI sweep: LU
+// factors without pivoting (forward multipliers l, 1/pivot dinv,
+// super-diagonal / pivot cu) and, periodic only, the Sherman-Morrison data.
+struct HostLineSys {
+  std::vector<double> l, dinv, cu, z;
+  double s0 = 0, s1 = 0;
+  int zA = 0, zB = 0, lo = 0, hi = 0, periodic = 0, n = 0;
+};
+// The CN system of one sweep axis (mat_CN / mat_CN_tridiagonal,
+// NS_functions.f90:1245-1342) for n cells with velocity code bc; normal: the
+// swept field is staggered along the axis (ns_api.cu).
+HostLineSys build_cn_system(int n, int bc, double h, double dt, double nu, bool normal, int closure,
+                            bool transposed = false);
 }  // namespace ns

@@ -1165,6 +1165,25 @@ def resimulate(st, cfg, knot_t, knot_data, t_start, n_intervals, sub_tstep=1, re
     return st
 
 
+def sweep_faces(u_d, v_d, w_d, d, bc):
+    """The faces of ADI sweep d (0 x, 1 y, 2 z) of a sub-block, from the
+    parent's sub-block u*, v*, w* after that sweep.  big_periodic_3D.f90:433-489
+    records them (bx_u_1s = u_star(idx_xu(1), ...), bx_v_1s = (v_star(idx_xv(1),
+    ...) + v_star(idx_xv(2), ...)) * 0.5d0, ...): the velocity part of
+    get_velpr_bc on the axis d only.  Returns a Faces with the axis-d keys."""
+    nx, ny, nz = u_d.shape[0] - 1, v_d.shape[1] - 1, w_d.shape[2] - 1
+    dummy = np.zeros((nx + 2, ny + 2, nz + 2))
+    b3 = [1, 1, 1]
+    b3[d] = bc
+    f = get_velpr_bc(u_d, v_d, w_d, dummy, tuple(b3), (1, 1, 1), 1.0, 1.0, 1.0, 0.0, 1, True, None)
+    out = Faces.zeros(nx, ny, nz)
+    a = "xyz"[d]
+    for k in out.d:
+        if k[0] == a and k[2] in "uvw":
+            out.d[k] = f.d[k]
+    return out
+
+
 def resimulate_frames(st, cfg, frames, p_prev0, using_ustar=True, dp_flag=1, restart=True):
     """Re-simulate one sub-block stepped at the parent's own time step, one
     parent record per step, with either boundary source of
@@ -1177,7 +1196,9 @@ def resimulate_frames(st, cfg, frames, p_prev0, using_ustar=True, dp_flag=1, res
     dp_flag = 0 (:506-508); faces from get_velpr_bc on u*_sub (using_Ustar)
     or u_sub (:510-520), whose u branch adds dt * diff(p_sub_pre) / h with
     dp_flag = 0 (NS_functions.f90:434-437); the DCT solve with the mean of
-    dp_sub (:766-768); p = dp_flag * p + dp (:801).
+    dp_sub (:766-768); p = dp_flag * p + dp (:801).  With AB2-CN a frame also
+    holds "cn": the faces of the three ADI sweeps (``sweep_faces``), the BC
+    rows of the sub-block's sweeps (:656-701).
     """
     dx, dy, dz = cfg.h
     st = st.copy()
@@ -1192,6 +1213,6 @@ def resimulate_frames(st, cfg, frames, p_prev0, using_ustar=True, dp_flag=1, res
             faces = get_velpr_bc(fr["u"], fr["v"], fr["w"], dp_sub, cfg.bc, cfg.pbc, dx, dy, dz, cfg.dt, dp_flag,
                                  False, p_sub_pre)
         c = dataclasses.replace(cfg, mean_dp=float(np.mean(dp_sub[1:-1, 1:-1, 1:-1])), gauge=0, dp_flag=dp_flag)
-        st = step(st, c, faces=faces)
+        st = step(st, c, faces=faces, cn_faces=fr.get("cn"))
         p_sub_pre = fr["p"]
     return st

@@ -194,3 +194,87 @@ def test_tgv_matches_the_oracle():
         np.testing.assert_allclose(got[k], ref, rtol=0, atol=4 * np.finfo(float).eps)
     only_p = tgv(x, y, nz, 0.0, 0.01, u=False, v=False)
     assert set(only_p) == {"p"}
+
+
+def _cn_parent(n=64, steps=3):
+    from ns_3d_staggered_dp_gb300 import Session, make_config
+    cfg = O.Config(n, n, n, nu=NU, dt=DT0, scheme=O.AB2_CN, dp_flag=1)
+    st = tgv_state(cfg, seed=5, noise=0.05)
+    s = Session(make_config(n, n, n, nu=NU, dt=DT0, scheme=O.AB2_CN, dp_flag=1, keep_sweeps=1))
+    s.set_state(st.u, st.v, st.w, st.p)
+    s.step(steps)
+    return s
+
+
+def test_ab2cn_batch_with_per_sweep_faces_replays_the_parent():
+    """AB2-CN re-simulation with the u* faces of every ADI sweep ("Ustar123",
+    big_periodic_3D.f90:433-489 records them, re_simulation_sub_tstep_interBC_combine.f90:656-701
+    takes them as the BC rows of the sub-block's dttrsb sweeps):
+    - every captured per-sweep face equals the oracle's record of the parent's
+      own post-sweep arrays bit for bit;
+    - restarted sub-blocks reproduce the parent's sub-blocks (property P1; the
+      reference logs 3.6e-14 in err_vel_AB2-CN_4.E-3_N_Ustar123_TOffset_restart.txt),
+      checked at 1e-11 relative L2;
+    - the oracle's re-simulation driven by the same faces agrees to 1e-10."""
+    from ns_3d_staggered_dp_gb300 import SWEEP_FACE_ORDER, Batch
+    subs = SUBS[:3]
+    parent = _cn_parent()
+    full = parent.get_state()
+    init = []
+    for x0, y0, z0, nx, ny, nz, _ in subs:
+        maps = O.subdomain_index_maps(x0, y0, z0, nx, ny, nz)
+        e = {k: O.extract_sub(full[k], k, maps) for k in ("u", "v", "w", "p")}
+        h = [O.extract_sub(full[k], f, maps) for k, f in (("hx", "u"), ("hy", "v"), ("hz", "w"))]
+        init.append(O.State(e["u"], e["v"], e["w"], e["p"], *h, first=False))
+    frames = [[] for _ in subs]
+    with Batch(subs, scheme=O.AB2_CN, bc=2, pbc=3, nu=NU, dt0=DT0, dx=H, dy=H, dz=H, n_slots=4, restart=1) as b:
+        b.init_from_parent(parent)
+        for n in range(1, 6):
+            parent.step(1)
+            slot = n % 4
+            b.capture(parent, slot, n * DT0)
+            sw = parent.get_sweeps()
+            stg = parent.get_stage()
+            ps = parent.get_state(history=False)
+            for i, (x0, y0, z0, nx, ny, nz, _) in enumerate(subs):
+                maps = O.subdomain_index_maps(x0, y0, z0, nx, ny, nz)
+                ex = lambda a, k: O.extract_sub(a, k, maps)
+                after = [(ex(sw["ux"], "u"), ex(sw["vx"], "v"), ex(sw["wx"], "w")),
+                         (ex(sw["uy"], "u"), ex(sw["vy"], "v"), ex(sw["wy"], "w")),
+                         (ex(stg["us"], "u"), ex(stg["vs"], "v"), ex(stg["ws"], "w"))]
+                cn = [O.sweep_faces(*after[d], d, 2) for d in range(3)]
+                got = b.get_sweep_faces(slot, i)
+                for k in SWEEP_FACE_ORDER:
+                    d = "xyz".index(k[0])
+                    assert np.array_equal(got[k], cn[d].d[k]), (n, i, k)
+                fr = {k: ex(ps[k], k) for k in ("u", "v", "w", "p")}
+                fr.update(us=after[2][0], vs=after[2][1], ws=after[2][2], dp=ex(stg["dp"], "p"), cn=cn)
+                frames[i].append(fr)
+            b.advance((n - 1) * DT0)
+        ps = parent.get_state(history=False)
+        for i, (x0, y0, z0, nx, ny, nz, _) in enumerate(subs):
+            maps = O.subdomain_index_maps(x0, y0, z0, nx, ny, nz)
+            got = b.get_state(i, history=False)
+            for k in ("u", "v", "w", "p"):
+                err = rel_l2(got[k], O.extract_sub(ps[k], k, maps))
+                assert err < 1e-11, ("P1", i, k, err)
+            cfg = O.Config(nx, ny, nz, lx=nx * H, ly=ny * H, lz=nz * H, nu=NU, dt=DT0, scheme=O.AB2_CN,
+                           bc=(2,) * 3, pbc=(3,) * 3, dp_flag=1, gauge=0)
+            ref = O.resimulate_frames(init[i], cfg, frames[i], init[i].p, using_ustar=True, dp_flag=1, restart=True)
+            for k in ("u", "v", "w", "p"):
+                err = rel_l2(got[k], getattr(ref, k))
+                assert err < STEP_TOL, ("oracle", i, k, err)
+            assert b.max_div(i) < 1e-10
+    parent.close()
+
+
+def test_ab2cn_batch_needs_a_keep_sweeps_parent():
+    from ns_3d_staggered_dp_gb300 import Batch, NSError
+    parent = _parent(1, n=32, steps=1)
+    with Batch([(1, 1, 1, 16, 16, 16, 1)], scheme=O.AB2_CN, bc=2, pbc=3, nu=NU, dt0=DT0, dx=H, dy=H, dz=H,
+               n_slots=4) as b:
+        with pytest.raises(NSError):
+            b.capture(parent, 0, 0.0)
+    with pytest.raises(NSError):
+        Batch([(1, 1, 1, 16, 16, 16, 2)], scheme=O.AB2_CN, bc=2, pbc=3, nu=NU, dt0=DT0, dx=H, dy=H, dz=H, n_slots=4)
+    parent.close()
