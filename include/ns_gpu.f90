@@ -90,6 +90,13 @@ module ns_gpu
       import :: c_ptr
     end function
 
+    ! the tile loader's bounded wait on a barrier no copy fills: NS_ERR_TIMEOUT is the expected answer
+    integer(c_int) function ns_selftest_wait_timeout(limit_ms, waited_ms) bind(C, name="ns_selftest_wait_timeout")
+      import :: c_int, c_double
+      real(c_double), value :: limit_ms
+      real(c_double), intent(out), optional :: waited_ms
+    end function
+
     integer(c_int) function ns_set_stream(h, stream) bind(C, name="ns_set_stream")
       import :: c_int, c_ptr
       type(c_ptr), value :: h

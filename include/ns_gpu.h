@@ -267,6 +267,16 @@ int ns_launch_count(const ns_handle* h, long long* launches);
 /* Version string of the library build. */
 const char* ns_version(void);
 
+/* Self-test of failure detection: the predictor's TMA tile loader waits on
+ * each ring slot's mbarrier with a bounded wait (NS_ERR_TIMEOUT through
+ * ns_get_diag when it gives up).  This call runs that same wait code on a
+ * barrier armed for bytes that no copy delivers, with a limit of limit_ms
+ * (0 < limit_ms <= 1000), and returns what the wait reported: NS_ERR_TIMEOUT
+ * is the expected answer (NS_OK would mean a wait that cannot end did);
+ * *waited_ms (may be NULL) receives the time the wait took.  Nothing is in
+ * flight when it gives up, and the device stays usable. */
+int ns_selftest_wait_timeout(double limit_ms, double* waited_ms);
+
 /* ------------------------------------------------------------------------
  * Batched tier: re-simulation of many sub-blocks of a parent run at once.
  *

@@ -87,6 +87,7 @@ SIGNATURES = {
     "ns_poisson_fft_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                          C.c_double, C.c_void_p]),
     "ns_version": (C.c_char_p, []),
+    "ns_selftest_wait_timeout": (C.c_int, [C.c_double, _DP]),
     "ns_batch_config_default": (None, [C.POINTER(NSBatchConfig)]),
     "ns_batch_create": (C.c_int, [C.POINTER(NSBatchConfig), C.POINTER(NSSubdomain), C.c_int, C.POINTER(C.c_void_p)]),
     "ns_batch_destroy": (C.c_int, [C.c_void_p]),

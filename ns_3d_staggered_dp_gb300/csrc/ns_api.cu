@@ -1011,6 +1011,31 @@ extern "C" {
 
 const char* ns_version(void) { return "ns_gpu 0.1 (sm_103a, FP64)"; }
 
+int ns_selftest_wait_timeout(double limit_ms, double* waited_ms) {
+  if (!(limit_ms > 0.0) || limit_ms > 1000.0) return NS_ERR_ARG;
+  int* d_gave = nullptr;
+  unsigned long long* d_ns = nullptr;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return NS_ERR_CUDA;
+  int status = NS_OK;
+  if (cudaMalloc(&d_gave, sizeof(int)) != cudaSuccess || cudaMalloc(&d_ns, sizeof(unsigned long long)) != cudaSuccess)
+    status = NS_ERR_NOMEM;
+  int gave = 0;
+  unsigned long long ns = 0;
+  if (!status && launch_wait_selftest((unsigned long long)(limit_ms * 1e6), d_gave, d_ns, st) != cudaSuccess)
+    status = NS_ERR_CUDA;
+  if (!status && (cudaMemcpyAsync(&gave, d_gave, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                  cudaMemcpyAsync(&ns, d_ns, sizeof(ns), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                  cudaStreamSynchronize(st) != cudaSuccess))
+    status = NS_ERR_CUDA;
+  if (d_gave) cudaFree(d_gave);
+  if (d_ns) cudaFree(d_ns);
+  cudaStreamDestroy(st);
+  if (status) return status;
+  if (waited_ms) *waited_ms = (double)ns * 1e-6;
+  return gave ? NS_ERR_TIMEOUT : NS_OK;
+}
+
 const char* ns_status_string(int s) {
   switch (s) {
     case NS_OK: return "ok";

@@ -187,6 +187,9 @@ struct AdiArgs {
   int z0, z1;                // x and y sweeps: only the lines of z slots [z0, z1) (z1 = 0: all)
 };
 cudaError_t launch_adi(int axis, const AdiArgs& a, cudaStream_t st);
+// The tile loader's bounded mbarrier wait on a barrier that no copy fills (ns_predict.cu).
+cudaError_t launch_wait_selftest(unsigned long long limit_ns, int* gave_up, unsigned long long* waited_ns,
+                                 cudaStream_t st);
 // One subdomain of the batched AB2-CN sweeps (ns_batch.cu): u*, v*, w* swept
 // in place (walls only), the nine line systems and the BC-row planes of each
 // sweep (the parent's per-sweep faces, big_periodic_3D.f90:433-489).

@@ -85,18 +85,42 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
-// Wait for the phase `parity` of a slot; false once kWaitLimit polls or
-// kWaitNs found it incomplete (the caller records the error).
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// Wait for the phase `parity` of a barrier; false once max_polls polls or
+// max_ns of global time found it incomplete (the caller records the error).
+__device__ __forceinline__ bool mbar_wait_for(unsigned long long* bar, unsigned parity, int max_polls,
+                                              unsigned long long max_ns) {
   // the common case (the plane has landed) reads no timer: a %globaltimer
   // read is a long-latency special-register access on every plane's path
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
-  for (int it = 0; it < kWaitLimit; ++it) {
+  for (int it = 0; it < max_polls; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 63) == 63 && global_ns() - t0 > kWaitNs) break;
+    if ((it & 63) == 63 && global_ns() - t0 > max_ns) break;
   }
   return false;
+}
+// The tile loader's wait: kWaitLimit polls or kWaitNs.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  return mbar_wait_for(bar, parity, kWaitLimit, kWaitNs);
+}
+
+// Self-test of the bounded wait: one thread arms a barrier for 8 bytes that
+// no copy will deliver and waits with the loader's wait code and a time limit
+// of limit_ns.  When the wait gives up (the expected outcome) the thread
+// delivers the 8 bytes itself (complete_tx), so the barrier's phase completes
+// before the CTA exits; nothing is in flight at any time.
+__global__ void wait_selftest_kernel(unsigned long long limit_ns, int* __restrict__ gave_up,
+                                     unsigned long long* __restrict__ waited_ns) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar);
+  const unsigned b = sm_addr(&bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(8u) : "memory");
+  const unsigned long long t0 = global_ns();
+  const bool ok = mbar_wait_for(&bar, 0, 1 << 22, limit_ns);
+  *waited_ns = global_ns() - t0;
+  if (!ok) asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(b), "r"(8u) : "memory");
+  *gave_up = ok ? 0 : 1;
 }
 // Fill ring slot s with plane k (clamped into the box) of u, v, w: x from slot
 // i0-2 (tensor x = slot + 7: 8 (32 bx + 6) bytes, 16-byte aligned), y from
@@ -456,6 +480,12 @@ static cudaError_t launch_t(const PredictArgs& a, cudaStream_t st, const PredTma
 }
 
 int predict_chunk_planes() { return KC; }
+
+cudaError_t launch_wait_selftest(unsigned long long limit_ns, int* gave_up, unsigned long long* waited_ns,
+                                 cudaStream_t st) {
+  wait_selftest_kernel<<<1, 32, 0, st>>>(limit_ns, gave_up, waited_ns);
+  return cudaGetLastError();
+}
 
 template <int SCHEME, bool FIRST, bool DPF>
 static cudaError_t launch_planes_t(PredictArgs b, cudaStream_t st, int p0, int p1, int kc, const PredTma* tma) {

@@ -289,3 +289,26 @@ def test_predictor_tile_loaders_agree(case, monkeypatch):
     for a, b in zip(res[0], res[1]):
         for k in a:
             assert np.array_equal(a[k], b[k]), k
+
+
+def test_bounded_tile_wait_gives_up_and_the_device_stays_usable():
+    """Failure detection of the predictor's TMA tile loader: its bounded
+    mbarrier wait, run on a barrier armed for bytes that no copy delivers,
+    gives up after the limit and reports NS_ERR_TIMEOUT; the context is
+    usable afterwards (a step still matches the oracle)."""
+    import ctypes
+
+    from ns_3d_staggered_dp_gb300 import _lib
+    lib = _lib.load()
+    waited = ctypes.c_double()
+    assert lib.ns_selftest_wait_timeout(5.0, ctypes.byref(waited)) == 4  # NS_ERR_TIMEOUT
+    assert 5.0 <= waited.value < 500.0, waited.value
+    assert lib.ns_selftest_wait_timeout(0.0, None) == 6  # NS_ERR_ARG
+    cfg = O.Config(16, 16, 16, nu=0.01, dt=0.01, scheme=O.AB2_CN)
+    st = tgv_state(cfg)
+    ref = O.step(st.copy(), cfg)
+    with session(cfg) as s:
+        s.set_state(st.u, st.v, st.w, st.p)
+        s.step(1)
+        got = s.get_state()
+    assert rel_l2(got["u"], ref.u) < 1e-10
