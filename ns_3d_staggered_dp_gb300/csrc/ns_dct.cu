@@ -604,24 +604,69 @@ __device__ __forceinline__ void tri_lines_body(const SpecPlan& S, double2* __res
     tri_real(x + 1, 2 * st, N, si, S.tri_elo, S.tri_ehi, rs, cm + (long long)N * TRI_T, false, 0.0);
     return;
   }
+  // Software-pipelined in groups of TP unknowns: the next group's values and
+  // multipliers are loaded before the current group is computed and stored,
+  // so no load waits behind a store of the same line (same operations, same
+  // bits as one unknown at a time).
+  constexpr int TP = 8;
   const double2* __restrict__ tm = S.tri_m + t;
+  double2 rv[TP], mv[TP];
+#pragma unroll
+  for (int q = 0; q < TP; ++q) {
+    const bool in = q < N;
+    rv[q] = in ? g[(long long)q * st] : make_double2(0.0, 0.0);
+    mv[q] = in ? __ldg(tm + (long long)q * st) : make_double2(0.0, 0.0);
+  }
   double2 d = make_double2(0.0, 0.0);
-#pragma unroll 4
-  for (int j = 0; j < N; ++j) {
-    const double2 mm = __ldg(tm + (long long)j * st);
-    const double2 r = g[(long long)j * st];
-    d.x = fma(r.x, rs, -d.x) * mm.x;
-    d.y = fma(r.y, rs, -d.y) * mm.y;
-    g[(long long)j * st] = d;
+  for (int j0 = 0; j0 < N; j0 += TP) {
+    double2 rn[TP], mn[TP];
+#pragma unroll
+    for (int q = 0; q < TP; ++q) {
+      const int j = j0 + TP + q;
+      const bool in = j < N;
+      rn[q] = in ? g[(long long)j * st] : make_double2(0.0, 0.0);
+      mn[q] = in ? __ldg(tm + (long long)j * st) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int q = 0; q < TP; ++q) {
+      const int j = j0 + q;
+      if (j < N) {
+        d.x = fma(rv[q].x, rs, -d.x) * mv[q].x;
+        d.y = fma(rv[q].y, rs, -d.y) * mv[q].y;
+        g[(long long)j * st] = d;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < TP; ++q) { rv[q] = rn[q]; mv[q] = mn[q]; }
   }
   double2 p = d;
-#pragma unroll 4
-  for (int j = N - 2; j >= 0; --j) {
-    const double2 mm = __ldg(tm + (long long)j * st);
-    const double2 x = g[(long long)j * st];
-    p.x = fma(-mm.x, p.x, x.x);
-    p.y = fma(-mm.y, p.y, x.y);
-    g[(long long)j * st] = p;
+#pragma unroll
+  for (int q = 0; q < TP; ++q) {
+    const int j = N - 2 - q;
+    const bool in = j >= 0;
+    rv[q] = in ? g[(long long)j * st] : make_double2(0.0, 0.0);
+    mv[q] = in ? __ldg(tm + (long long)j * st) : make_double2(0.0, 0.0);
+  }
+  for (int j0 = N - 2; j0 >= 0; j0 -= TP) {
+    double2 rn[TP], mn[TP];
+#pragma unroll
+    for (int q = 0; q < TP; ++q) {
+      const int j = j0 - TP - q;
+      const bool in = j >= 0;
+      rn[q] = in ? g[(long long)j * st] : make_double2(0.0, 0.0);
+      mn[q] = in ? __ldg(tm + (long long)j * st) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int q = 0; q < TP; ++q) {
+      const int j = j0 - q;
+      if (j >= 0) {
+        p.x = fma(-mv[q].x, p.x, rv[q].x);
+        p.y = fma(-mv[q].y, p.y, rv[q].y);
+        g[(long long)j * st] = p;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < TP; ++q) { rv[q] = rn[q]; mv[q] = mn[q]; }
   }
 }
 
