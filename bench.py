@@ -408,7 +408,10 @@ def run_resim(args):
     kernels launched once per subdomain and stage (mode 1), and (2) the plain
     path: one session per subdomain, advanced one by one with ns_set_faces,
     ns_set_mean_dp and ns_step, the faces of each interval read back from the
-    batch's snapshots beforehand (untimed)."""
+    batch's snapshots beforehand (untimed).  --resim-scheme ab2cn runs the
+    AB2-CN re-simulation instead: parent and sub-blocks AB2-CN, the sub-blocks'
+    ADI sweeps bounded by the parent's u* after each sweep, sub_tstep 1 (the
+    reference's restriction for AB2-CN)."""
     import torch
     from ns_3d_staggered_dp_gb300 import Batch, Session, make_config
 
@@ -416,11 +419,15 @@ def run_resim(args):
     torch.cuda.set_device(local)
     n = 128
     T = args.steps
+    cn = getattr(args, "resim_scheme", "ab2") == "ab2cn"
+    scheme = 2 if cn else 1
     u, v, w, p, umax = hit_initial_field(n, seed=64)
     nu = 1.0 / 1600.0
     h = 2 * np.pi / n
     dt = 0.3 * h / umax
     subs = resim_subdomains(n)
+    if cn:
+        subs = [s[:6] + (1,) for s in subs]
     cells = [nx * ny * nz for (_, _, _, nx, ny, nz, _) in subs]
     # cell-steps of the run: the first interval takes sub_tstep sub-steps
     work = sum(c * (r + (T - 1)) for c, (*_, r) in zip(cells, subs))
@@ -429,10 +436,10 @@ def run_resim(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     out = {}
-    with Session(make_config(n, n, n, nu=nu, dt=dt, scheme=1, dp_flag=1)) as par:
+    with Session(make_config(n, n, n, nu=nu, dt=dt, scheme=scheme, dp_flag=1, keep_sweeps=int(cn))) as par:
         par.set_stream(stream.cuda_stream)
         par.set_state(u, v, w, p)
-        batches = {m: Batch(subs, scheme=1, bc=2, pbc=3, nu=nu, dt0=dt, dx=h, dy=h, dz=h, n_slots=n_slots,
+        batches = {m: Batch(subs, scheme=scheme, bc=2, pbc=3, nu=nu, dt0=dt, dx=h, dy=h, dz=h, n_slots=n_slots,
                             mode=m, use_graph=1) for m in (0, 1)}
         for b in batches.values():
             b.set_stream(stream.cuda_stream)
@@ -467,7 +474,7 @@ def run_resim(args):
             out[m] = {"ms": ms, "value": steady / (ms / 1e3), "launches": b.launch_count() - l0,
                       "clocks": clk.summary()}
         job_sec = time.perf_counter() - t_job0
-        plain = run_plain_loop(subs, init_states, batches[0], stream, n0, T, nu, dt, h)
+        plain = run_plain_loop(subs, init_states, batches[0], stream, n0, T, nu, dt, h, cn=cn)
         stage_ms = batches[0].profile(reps=3)
         st = [batches[m].get_state(0, history=False) for m in (0, 1)]
         same = all(np.array_equal(st[0][k], st[1][k]) for k in ("u", "v", "w", "p"))
@@ -477,12 +484,15 @@ def run_resim(args):
     if rank != 0:
         return None
     line = {
-        "metric": "FP64 subdomain cell-steps/s, batched re-simulation of 64 sub-blocks (128^3 periodic parent)",
+        "metric": ("FP64 subdomain cell-steps/s, batched re-simulation of 64 sub-blocks (128^3 periodic parent)"
+                   + (", AB2-CN with per-sweep u* faces" if cn else "")),
         "value": out[0]["value"], "unit": UNIT, "n_gpus": world, "steps": T - 1, "warmup": 1,
         "ms_per_step": out[0]["ms"] / (T - 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded k^4 exp(-2(k/4)^2) parent field, seed 64)",
-        "config": {"workload": "64 sub-blocks, edges {16,24,32,48,64} and sub_tstep {1,2,4} (seed 4096), "
-                               "AB2, bc 2 / pbc 3, dp_flag 1, u* BCs, spline-interpolated parent snapshots",
+        "config": {"workload": ("64 sub-blocks, edges {16,24,32,48,64} (seed 4096), AB2-CN, sub_tstep 1, bc 2 / "
+                                "pbc 3, dp_flag 1, u* BCs of every ADI sweep, parent snapshots every step" if cn else
+                                "64 sub-blocks, edges {16,24,32,48,64} and sub_tstep {1,2,4} (seed 4096), "
+                                "AB2, bc 2 / pbc 3, dp_flag 1, u* BCs, spline-interpolated parent snapshots"),
                    "parent": [n, n, n], "subdomain_cells": int(sum(cells)), "intervals": T,
                    "first_interval_substeps": True},
         "loop": {"value": out[1]["value"], "ms_per_step": out[1]["ms"] / (T - 1), "launches": out[1]["launches"],
@@ -503,7 +513,7 @@ def run_resim(args):
     return line
 
 
-def run_plain_loop(subs, init_states, batch, stream, n0, T, nu, dt, h):
+def run_plain_loop(subs, init_states, batch, stream, n0, T, nu, dt, h, cn=False):
     """The plain path of the re-simulation: one session per subdomain (DCT
     pressure solve of the all-wall box), stepped one subdomain after another
     with its faces and mean dp for the interval (ns_set_faces, ns_set_mean_dp,
@@ -520,7 +530,7 @@ def run_plain_loop(subs, init_states, batch, stream, n0, T, nu, dt, h):
     sess = []
     try:
         for (x0, y0, z0, nx, ny, nz, r), st in zip(subs, init_states):
-            s = Session(make_config(nx, ny, nz, lx=nx * h, ly=ny * h, lz=nz * h, nu=nu, dt=dt, scheme=1,
+            s = Session(make_config(nx, ny, nz, lx=nx * h, ly=ny * h, lz=nz * h, nu=nu, dt=dt, scheme=2 if cn else 1,
                                     bc=(2, 2, 2), pbc=(3, 3, 3), dp_flag=1, gauge=0))
             s.set_stream(stream.cuda_stream)
             s.set_state(st["u"], st["v"], st["w"], st["p"], (st["hx"], st["hy"], st["hz"]))
@@ -535,14 +545,22 @@ def run_plain_loop(subs, init_states, batch, stream, n0, T, nu, dt, h):
             for i, s in enumerate(sess):
                 faces, mean = batch.get_snapshot(slot, i)
                 keep = [np.asfortranarray(faces[k]) for k in FACE_ORDER]
-                arr = (P * 24)(*[a.ctypes.data_as(P) for a in keep])
-                prepared.append((s.h, arr, keep, mean))
+                arrs = [(P * 24)(*[a.ctypes.data_as(P) for a in keep])]
+                if cn:  # the per-sweep faces go in face sets 1-3 (axis d's u, v, w entries)
+                    sw = batch.get_sweep_faces(slot, i)
+                    for d in range(3):
+                        ks = [k if k[0] == "xyz"[d] and k[2] in "uvw" else None for k in FACE_ORDER]
+                        a_d = [np.asfortranarray(sw[k]) if k else None for k in ks]
+                        keep += [a for a in a_d if a is not None]
+                        arrs.append((P * 24)(*[a.ctypes.data_as(P) if a is not None else None for a in a_d]))
+                prepared.append((s.h, arrs, keep, mean))
             l0 = sum(s.launch_count() for s in sess)
             torch.cuda.synchronize()
             e0.record(stream)
             rcs = 0
-            for hh, arr, _keep, mean in prepared:
-                rcs |= lib.ns_set_faces(hh, 0, arr)
+            for hh, arrs, _keep, mean in prepared:
+                for which, arr in enumerate(arrs):
+                    rcs |= lib.ns_set_faces(hh, which, arr)
                 rcs |= lib.ns_set_mean_dp(hh, mean)
                 rcs |= lib.ns_step(hh, 1)
             e1.record(stream)
@@ -563,7 +581,8 @@ def run_plain_loop(subs, init_states, batch, stream, n0, T, nu, dt, h):
         return {"ms_per_step": ms / max(1, timed), "value": cells * timed / (ms / 1e3) if ms > 0 else None,
                 "intervals_timed": timed, "launches": launches, "max_rel_l2_vs_batched": diff,
                 "what": "64 sessions (ns_create with the subdomain's box, DCT/DST pressure solve), each interval "
-                        "ns_set_faces + ns_set_mean_dp + ns_step(1) per subdomain, one after another"}
+                        "ns_set_faces (set 0, and sets 1-3 with AB2-CN) + ns_set_mean_dp + ns_step(1) per "
+                        "subdomain, one after another"}
     finally:
         for s in sess:
             s.close()
@@ -891,6 +910,16 @@ def run_ours(args):
             line["batched"] = {"error": str(e)}
         try:
             a = argparse.Namespace(**vars(args))
+            a.steps, a.autotune, a.resim_scheme = 20, False, "ab2cn"
+            r = run_resim(a)
+            line["batched_ab2cn"] = {k: r[k] for k in ("metric", "value", "ms_per_step", "speedup_vs_plain_path_loop",
+                                                       "speedup_vs_loop", "bitwise_equal_to_loop", "max_div")} | {
+                "plain_path_loop_ms_per_step": r["plain_path_loop"].get("ms_per_step"),
+                "plain_path_max_rel_l2_vs_batched": r["plain_path_loop"].get("max_rel_l2_vs_batched")}
+        except Exception as e:
+            line["batched_ab2cn"] = {"error": str(e)}
+        try:
+            a = argparse.Namespace(**vars(args))
             a.adj_dirs = 32
             r = run_adjoint(a)
             line["adjoint"] = {k: r[k] for k in ("metric", "value", "forward_ms_per_step", "backward_ms_per_step",
@@ -938,6 +967,8 @@ def main():
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="skip the batched and adjoint summaries of the default line")
     ap.add_argument("--autotune", action="store_true", help="resim: autotune the batched stage kernels first")
+    ap.add_argument("--resim-scheme", default="ab2", choices=["ab2", "ab2cn"],
+                    help="resim: AB2 (sub-steps, spline BCs) or AB2-CN (per-sweep u* BCs, sub_tstep 1)")
     args = ap.parse_args()
     if args.workload in ("resim", "adjoint") and args.impl != "reference":
         line = run_resim(args) if args.workload == "resim" else run_adjoint(args)
