@@ -299,11 +299,96 @@ __global__ void __launch_bounds__(kAdiBatchLines) adi_batch_kernel(const BatchAd
   }
 }
 
+// The batched x sweep with the session x sweep's staging: each warp of an
+// item takes 32 of its 128 lines and walks them in blocks of 32 unknowns
+// through shared memory, so every global access is a coalesced row segment
+// (the lines are contiguous, the lanes of the one-thread-per-line kernel
+// would stride across rows).  Same operations as adi_batch_kernel.
+__global__ void __launch_bounds__(kAdiBatchLines) adi_batch_x_kernel(const BatchAdiArgs* __restrict__ tab,
+                                                                     const BatchItem* __restrict__ items, int n_items) {
+  constexpr int NW = kAdiBatchLines / 32;
+  __shared__ double sh[NW][XB * XS];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  double* sb = sh[warp];
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    const BatchAdiArgs& A = tab[w.sub];
+    const Layout L = A.L;
+    const int fld = w.by;
+    const LineSys& S = A.sys[0][fld];
+    const int n1 = L.ny + 2;
+    const int nlines = n1 * (L.nz + 2);
+    const int t0 = w.bx * kAdiBatchLines + warp * 32;
+    if (t0 >= nlines) continue;  // warp-uniform
+    const int nl = min(32, nlines - t0);
+    const int t = t0 + min(lane, nl - 1);  // lanes past the end repeat the last line (never stored)
+    const int j = t % n1, k = t / n1;
+    const int my_off = (int)L.at(S.lo, j, k);
+    double* f = A.f[fld];
+    const double* lf = S.l + S.pad;
+    const double* di = S.dinv + S.pad;
+    const double* cu = S.cu + S.pad;
+    const int m = S.hi - S.lo + 1;
+    const int nb = (m + XB - 1) / XB;
+    const bool act = lane < nl;
+    const double face_lo = (act && A.face_lo[0][fld]) ? __ldg(A.face_lo[0][fld] + t) : 0.0;
+    const double face_hi = (act && A.face_hi[0][fld]) ? __ldg(A.face_hi[0][fld] + t) : 0.0;
+    double yp = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      const int e0 = b * XB;
+      const int ne = min(XB, m - e0);
+#pragma unroll 8
+      for (int l = 0; l < XB; ++l) {
+        const int off = __shfl_sync(0xffffffffu, my_off, l);
+        if (l < nl && lane < ne) sb[lane * XS + l] = f[off + e0 + lane];
+      }
+      __syncwarp();
+      if (e0 == 0) sb[lane] = face_lo;  // the BC rows take the sweep's face values
+      if (m - 1 - e0 < XB) sb[(m - 1 - e0) * XS + lane] = face_hi;
+      if (act)
+        for (int q = 0; q < ne; ++q) {
+          yp = fma(-__ldg(lf + e0 + q), yp, sb[q * XS + lane]);
+          sb[q * XS + lane] = yp;
+        }
+      __syncwarp();
+#pragma unroll 8
+      for (int l = 0; l < XB; ++l) {
+        const int off = __shfl_sync(0xffffffffu, my_off, l);
+        if (l < nl && lane < ne) f[off + e0 + lane] = sb[lane * XS + l];
+      }
+      __syncwarp();
+    }
+    double xn = 0.0;
+    for (int b = nb - 1; b >= 0; --b) {
+      const int e0 = b * XB;
+      const int ne = min(XB, m - e0);
+#pragma unroll 8
+      for (int l = 0; l < XB; ++l) {
+        const int off = __shfl_sync(0xffffffffu, my_off, l);
+        if (l < nl && lane < ne) sb[lane * XS + l] = f[off + e0 + lane];
+      }
+      __syncwarp();
+      if (act)
+        for (int q = ne - 1; q >= 0; --q) {
+          xn = fma(-__ldg(cu + e0 + q), xn, sb[q * XS + lane] * __ldg(di + e0 + q));
+          sb[q * XS + lane] = xn;
+        }
+      __syncwarp();
+#pragma unroll 8
+      for (int l = 0; l < XB; ++l) {
+        const int off = __shfl_sync(0xffffffffu, my_off, l);
+        if (l < nl && lane < ne) f[off + e0 + lane] = sb[lane * XS + l];
+      }
+      __syncwarp();
+    }
+  }
+}
+
 cudaError_t launch_adi_batch(int axis, const BatchAdiArgs* tab, const BatchItem* items, int n_items, int grid,
                              cudaStream_t st) {
   if (n_items <= 0) return cudaSuccess;
   grid = std::max(1, std::min(grid, n_items));
-  if (axis == 0) adi_batch_kernel<0><<<grid, kAdiBatchLines, 0, st>>>(tab, items, n_items);
+  if (axis == 0) adi_batch_x_kernel<<<grid, kAdiBatchLines, 0, st>>>(tab, items, n_items);
   else if (axis == 1) adi_batch_kernel<1><<<grid, kAdiBatchLines, 0, st>>>(tab, items, n_items);
   else adi_batch_kernel<2><<<grid, kAdiBatchLines, 0, st>>>(tab, items, n_items);
   return cudaGetLastError();
