@@ -1,6 +1,8 @@
 """CPU checks of the oracle itself (no GPU): the reference's own self-checks
 restated, the operator identities the spectral solvers must satisfy, and the
 accuracy properties the reference logs in err_file/."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -194,3 +196,81 @@ def test_power_spec_single_mode_and_parseval():
     assert E[1] > 0 and np.all(np.abs(others) < 1e-25 * E[1])
     p = O.spec_prop(E, k, 0.01, u, z, z, n, dk, m)
     assert abs(p["kin_E"] - p["kin_Ph"]) < 1e-14 and abs(p["kin_Ph"] - 0.25) < 1e-14
+
+
+def test_sweep_faces_are_the_parent_records():
+    """O.sweep_faces restates the per-sweep records of big_periodic_3D.f90:433-489
+    on a sub-block: after the x sweep bx_u_1s = u_star(idx_xu(1), ...),
+    bx_v_1s = (v_star(idx_xv(1), ...) + v_star(idx_xv(2), ...)) * 0.5d0, ...;
+    only the swept axis's velocity faces are set."""
+    rng = np.random.default_rng(11)
+    nx, ny, nz = 6, 5, 4
+    u = rng.standard_normal((nx + 1, ny + 2, nz + 2))
+    v = rng.standard_normal((nx + 2, ny + 1, nz + 2))
+    w = rng.standard_normal((nx + 2, ny + 2, nz + 1))
+    fx = O.sweep_faces(u, v, w, 0, 2)
+    assert np.array_equal(fx.d["x_u_1"], u[0]) and np.array_equal(fx.d["x_u_n"], u[nx])
+    assert np.array_equal(fx.d["x_v_1"], (v[0] + v[1]) * 0.5)
+    assert np.array_equal(fx.d["x_w_n"], (w[nx + 1] + w[nx]) * 0.5)
+    assert not fx.d["y_u_1"].any() and not fx.d["x_p_1"].any()
+    fy = O.sweep_faces(u, v, w, 1, 2)
+    assert np.array_equal(fy.d["y_u_1"], (u[:, 0] + u[:, 1]) * 0.5)
+    assert np.array_equal(fy.d["y_v_n"], v[:, ny])
+    fz = O.sweep_faces(u, v, w, 2, 2)
+    assert np.array_equal(fz.d["z_w_1"], w[:, :, 0]) and np.array_equal(fz.d["z_w_n"], w[:, :, nz])
+    assert np.array_equal(fz.d["z_v_n"], (v[:, :, nz + 1] + v[:, :, nz]) * 0.5)
+
+
+def test_velpr_bc_u_branch_adds_the_previous_pressure_gradient():
+    """get_velpr_bc with u boundary values and dp_flag = 0 adds
+    dt * diff(p_previous) / h to the velocity before taking the faces
+    (NS_functions.f90:434-437); with u* or dp_flag = 1 it does not."""
+    rng = np.random.default_rng(12)
+    nx, ny, nz = 6, 5, 4
+    u = rng.standard_normal((nx + 1, ny + 2, nz + 2))
+    v = rng.standard_normal((nx + 2, ny + 1, nz + 2))
+    w = rng.standard_normal((nx + 2, ny + 2, nz + 1))
+    p = rng.standard_normal((nx + 2, ny + 2, nz + 2))
+    pp = rng.standard_normal((nx + 2, ny + 2, nz + 2))
+    h, dt = 0.1, 0.01
+    f0 = O.get_velpr_bc(u, v, w, p, (2, 2, 2), (3, 3, 3), h, h, h, dt, 0, False, pp)
+    uc = u + O.diff(pp, 1, 1) / h * dt
+    vc = v + O.diff(pp, 1, 2) / h * dt
+    assert np.array_equal(f0.d["x_u_1"], uc[0])
+    assert np.array_equal(f0.d["y_u_n"], (uc[:, ny + 1] + uc[:, ny]) / 2)
+    assert np.array_equal(f0.d["x_v_1"], (vc[0] + vc[1]) / 2)
+    for dpf, ustar in ((1, False), (0, True)):
+        f1 = O.get_velpr_bc(u, v, w, p, (2, 2, 2), (3, 3, 3), h, h, h, dt, dpf, ustar, pp)
+        assert np.array_equal(f1.d["x_u_1"], u[0])
+    # the pressure faces come from the pressure argument either way (get_pr_bc)
+    assert np.array_equal(f0.d["x_p_1"], (p[1] - p[0]) / h)
+
+
+def test_resimulate_frames_steps_with_the_frame_faces():
+    """resimulate_frames follows re_simulation_sub_tstep_interBC_combine.f90:436-801:
+    one step per frame with that frame's faces and the mean of its pressure
+    source, p_sub_pre carried from frame to frame."""
+    cfg = O.Config(8, 8, 8, lx=1.0, ly=1.0, lz=1.0, nu=0.01, dt=1e-3, scheme=O.AB2, bc=(2,) * 3, pbc=(3,) * 3,
+                   dp_flag=0, gauge=0)
+    rng = np.random.default_rng(13)
+    st = O.State.zeros(8, 8, 8)
+    st.u = 0.1 * rng.standard_normal(st.u.shape); st.v = 0.1 * rng.standard_normal(st.v.shape)
+    st.w = 0.1 * rng.standard_normal(st.w.shape)
+    st.first = False
+    frames = []
+    for _ in range(2):
+        fr = {k: 0.1 * rng.standard_normal(getattr(st, k).shape) for k in ("u", "v", "w", "p")}
+        fr.update(us=fr["u"], vs=fr["v"], ws=fr["w"], dp=fr["p"])
+        frames.append(fr)
+    p0 = 0.1 * rng.standard_normal(st.p.shape)
+    got = O.resimulate_frames(st, cfg, frames, p0, using_ustar=False, dp_flag=0, restart=True)
+    ref = st.copy()
+    prev = p0
+    h = cfg.h[0]
+    for fr in frames:
+        faces = O.get_velpr_bc(fr["u"], fr["v"], fr["w"], fr["p"], cfg.bc, cfg.pbc, h, h, h, cfg.dt, 0, False, prev)
+        c = dataclasses.replace(cfg, mean_dp=float(np.mean(fr["p"][1:-1, 1:-1, 1:-1])))
+        ref = O.step(ref, c, faces=faces)
+        prev = fr["p"]
+    for k in ("u", "v", "w", "p"):
+        assert np.array_equal(getattr(got, k), getattr(ref, k))
