@@ -459,7 +459,7 @@ int validate(const ns_config& c, std::string& msg) {
       msg = "the wall axis solved by lines is limited to 512 cells (256 with a wall x)";
       return NS_ERR_SHAPE;
     }
-    if (a == 1 && a != sax && n3[a] > 128) { msg = "a wall y in front of a wall z is limited to 128 cells"; return NS_ERR_SHAPE; }
+    if (a == 1 && a != sax && n3[a] > 512) { msg = "a wall y in front of a wall z is limited to 512 cells"; return NS_ERR_SHAPE; }
     if (a == 0 && (n3[a] % 2 != 0 || n3[a] > 1024)) {
       msg = "a non-periodic x axis needs an even cell count <= 1024";
       return NS_ERR_SHAPE;
@@ -912,7 +912,19 @@ int build_plans(ns_handle* h) {
   // lines and 32 warps per SM the division chain is hidden, and a table
   // (the batched solve's choice, launch_tri_table) only adds a second load
   // stream (256x128x256 y solve: 0.28 ms computed, 0.37 ms from a table).
+  // A packed-x (all-wall) box's z solve keeps two multipliers per line in
+  // shared memory, 2 nz x 32 doubles a warp, which at nz = 256 leaves one
+  // warp per SM: it reads them from a table instead (same bits).
   P.tri_m = nullptr;
+  P.sing_cm = nullptr;
+  if (sax == 2 && P.kind[0] == 1) {
+    NS_CUDA(h, cudaMalloc(&h->tri_tab, (size_t)nxs * ny * nz * sizeof(double2)));
+    NS_CUDA(h, cudaMalloc(&h->sing_cm, (size_t)2 * nz * 32 * sizeof(double)));
+    NS_CUDA(h, launch_tri_table(2, P, h->tri_tab, h->stream));
+    NS_CUDA(h, cudaStreamSynchronize(h->stream));
+    P.tri_m = h->tri_tab;
+    P.sing_cm = h->sing_cm;
+  }
   return NS_OK;
 }
 
@@ -966,6 +978,8 @@ void free_all(ns_handle* h) {
     if (b) cudaFree(b);
   if (h->spec) cudaFree(h->spec);
   if (h->mean_dev) cudaFree(h->mean_dev);
+  if (h->tri_tab) cudaFree(h->tri_tab);
+  if (h->sing_cm) cudaFree(h->sing_cm);
   if (h->cyc_buf) cudaFree(h->cyc_buf);
   if (h->stage) cudaFree(h->stage);
   if (h->stage2) cudaFree(h->stage2);

@@ -776,13 +776,16 @@ int dense_symmetry(int n, const std::vector<double>& F, const std::vector<double
 
 cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st) {
   const int N = axis == 1 ? S.ny : S.nz;
-  if (N > 128) return cudaErrorInvalidValue;
+  if (N > 512) return cudaErrorInvalidValue;
+  // 16 lines of N complex values staged in shared memory: 32 KB at N = 128,
+  // 128 KB at 512 (past the 48 KB default: opt in)
   const size_t sm = (size_t)N * 16 * sizeof(double2);
   dim3 grid((S.nxs * (axis == 1 ? S.nz : S.ny) + 15) / 16);
-  if (axis == 1 && fwd) dense_yz_kernel<1, true><<<grid, 128, sm, st>>>(S, spec);
-  else if (axis == 1) dense_yz_kernel<1, false><<<grid, 128, sm, st>>>(S, spec);
-  else if (fwd) dense_yz_kernel<2, true><<<grid, 128, sm, st>>>(S, spec);
-  else dense_yz_kernel<2, false><<<grid, 128, sm, st>>>(S, spec);
+  auto kern = (axis == 1) ? (fwd ? dense_yz_kernel<1, true> : dense_yz_kernel<1, false>)
+                          : (fwd ? dense_yz_kernel<2, true> : dense_yz_kernel<2, false>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, 128, sm, st>>>(S, spec);
   return cudaGetLastError();
 }
 
@@ -802,10 +805,20 @@ cudaError_t launch_tri_table(int axis, const SpecPlan& S, double2* tab, cudaStre
   return cudaGetLastError();
 }
 
+// The session's table-driven z solve of a packed-x box: 128 lines per CTA,
+// no shared memory (the singular line's multipliers go to S.sing_cm).
+__global__ void __launch_bounds__(128) tri_lines_kernel(SpecPlan S, double2* __restrict__ spec) {
+  tri_lines_body(S, spec, S.sing_cm, blockIdx.x);
+}
+
 cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st) {
   const int N = axis == 1 ? S.ny : S.nz;
   const int n_other = axis == 1 ? S.nz : S.ny;
   const bool packed = S.kind[0] != 0;
+  if (axis == 2 && packed && S.tri_m && S.sing_cm) {
+    tri_lines_kernel<<<(S.nxs * S.ny + 127) / 128, 128, 0, st>>>(S, spec);
+    return cudaGetLastError();
+  }
   const size_t sm = (size_t)N * TRI_T * sizeof(double) * (packed ? 2 : 1);
   if (sm > 200 * 1024) return cudaErrorInvalidValue;
   const int nreg = packed ? S.nxs : S.nxs - 1;

@@ -233,7 +233,9 @@ struct FftPlan {
   double tri_rs;          // h_s^2 * scale of the unnormalised FFT passes
   double tri_elo, tri_ehi;  // end-row diagonal changes: pbc 2 -1, pbc 3 +1, pbc 4 0
   const double2* tri_m;   // the forward multipliers (re, im) of every line, laid out like the spectrum
-                          // (launch_tri_table); read by the batched z solve (tri_lines_body)
+                          // (launch_tri_table); read by the table-driven z solve (tri_lines_body)
+  double* sing_cm;        // session z solve from the table: global scratch (2 nz TRI_T doubles) of the
+                          // singular line's multipliers (the batch keeps them in shared memory)
   // All-periodic boxes: the z stage as cyclic tridiagonal line solves (ns_cyclic.cu)
   // instead of z FFT * 1/lambda * z IFFT.  Tables per (kx, ky) mode, laid out like the
   // spectrum: T's multipliers, w = rs T^-1 e0, q = T^-1 u; per mode (1/c, SM denominator).

@@ -56,10 +56,13 @@ POISSON_CASES = [
     ((16, 32, 256), (1, 1, 2)),
     ((32, 128, 200), (1, 4, 3)),
     ((64, 64, 64), (3, 3, 3)),
-    # the size limits: the wall axis solved by lines (512), a dense y in front of it (128),
-    # a dense x (1024, with its line axis limited to 256)
+    # the size limits: the wall axis solved by lines (512), a dense y in front of it (512:
+    # past 128 its line buffer needs the opt-in shared memory), a dense x (1024, with its
+    # line axis limited to 256)
     ((16, 16, 512), (1, 1, 3)),
     ((16, 128, 512), (1, 2, 4)),
+    ((16, 200, 16), (3, 3, 3)),
+    ((16, 512, 16), (1, 2, 3)),
     ((1024, 16, 16), (3, 3, 3)),
 ]
 
@@ -157,6 +160,18 @@ def test_step_open_box_faces(scheme, dp_flag):
     _run_compare(cfg, st, 6, faces=faces, cn_faces=cn_faces, div_free=False)
 
 
+def test_step_all_wall_box_with_a_long_dense_y():
+    """An all-wall box whose dense y transform is longer than 128 points (the
+    line buffer of the y passes then opts in to more shared memory): AB2-CN
+    steps with wall faces against the oracle."""
+    cfg = O.Config(16, 192, 24, lx=0.5, ly=6.0, lz=0.75, nu=0.01, dt=1e-3, scheme=O.AB2_CN, bc=(2, 2, 2),
+                   pbc=(3, 3, 3), dp_flag=1, mean_dp=0.02)
+    faces = random_faces(cfg, 21, amp=0.1)
+    cn_faces = [random_faces(cfg, 22 + d, amp=0.1) for d in range(3)]
+    st = random_state(cfg, 23, amp=0.2)
+    _run_compare(cfg, st, 4, faces=faces, cn_faces=cn_faces, div_free=False)
+
+
 @pytest.mark.parametrize("bc,pbc", [((4, 2, 4), (4, 2, 4)), ((2, 4, 2), (2, 3, 2)), ((2, 2, 4), (3, 2, 4))])
 def test_step_wall_codes(bc, pbc):
     """Dirichlet-on-the-ghost (4) and Dirichlet-on-the-wall (2) codes mixed,
@@ -187,7 +202,7 @@ def test_unsupported_mixes_rejected():
     bad = [
         dict(nx=32, ny=16, nz=32, bc=(2, 1, 1), pbc=(3, 1, 1)),   # wall x with periodic y/z
         dict(nx=32, ny=1024, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),  # line-solved y longer than 512
-        dict(nx=32, ny=256, nz=32, bc=(1, 2, 2), pbc=(1, 3, 3)),   # dense y (wall z behind it) over 128
+        dict(nx=32, ny=640, nz=32, bc=(1, 2, 2), pbc=(1, 3, 3)),   # dense y (wall z behind it) over 512
         dict(nx=24, ny=16, nz=32, bc=(1, 2, 1), pbc=(1, 3, 1)),   # FFT x not a power of two
         dict(nx=25, ny=16, nz=32, bc=(2, 2, 2), pbc=(3, 3, 3)),   # odd wall x
     ]
