@@ -784,6 +784,28 @@ int build_plans(ns_handle* h) {
   if (P.kind[1] == 0) twid(ny, ny, tw);
   o_z = tw.size();
   if (P.kind[2] == 0) twid(nz, nz, tw);
+  // A dense y (in front of a wall z) of power-of-two length >= 32 with pbc 2
+  // or 3 goes through an FFT: its twiddles and the DCT pre/post-twiddles.
+  // (NS_DENSE_Y in the environment keeps the dense products, for comparison.)
+  P.dct_y = 0;
+  size_t o_dtw = 0, o_dwf = 0, o_dwi = 0;
+  if (P.kind[1] == 1 && (c.pbc[1] == 2 || c.pbc[1] == 3) && ny >= 32 && ny <= 512 &&
+      (ny & (ny - 1)) == 0 && !std::getenv("NS_DENSE_Y")) {
+    P.dct_y = c.pbc[1];
+    const long double pi = 3.141592653589793238462643383279502884L;
+    o_dtw = tw.size();
+    twid(ny, ny, tw);
+    o_dwf = tw.size();
+    for (int k = 0; k <= ny; ++k) {
+      const long double th = pi * (long double)k / (2.0L * ny);
+      tw.push_back(make_double2((double)(cosl(th) / 2.0L), (double)(-sinl(th) / 2.0L)));
+    }
+    o_dwi = tw.size();
+    for (int k = 0; k < ny; ++k) {
+      const long double th = pi * (long double)k / (2.0L * ny);
+      tw.push_back(make_double2((double)(cosl(th) / ny), (double)(sinl(th) / ny)));
+    }
+  }
   if (tw.empty()) tw.push_back(make_double2(1.0, 0.0));
   NS_CUDA(h, cudaMalloc(&h->tw, tw.size() * sizeof(double2)));
   NS_CUDA(h, cudaMemcpyAsync(h->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
@@ -881,6 +903,9 @@ int build_plans(ns_handle* h) {
   const double* t0 = h->inv_lam;
   P.nx = nx; P.ny = ny; P.nz = nz; P.nxh = nxh; P.nxs = nxs;
   P.tw_x = h->tw; P.tw_xr = h->tw + o_xr; P.tw_y = h->tw + o_y; P.tw_z = h->tw + o_z;
+  P.dct_tw = P.dct_y ? h->tw + o_dtw : nullptr;
+  P.dct_wf = P.dct_y ? h->tw + o_dwf : nullptr;
+  P.dct_wi = P.dct_y ? h->tw + o_dwi : nullptr;
   const bool zcyc = !sax && allper && c.poisson_z == 0;
   P.inv_lam = (sax || zcyc) ? nullptr : t0 + o_il;
   P.eig_x = (sax || zcyc) ? t0 + o_ex : nullptr;

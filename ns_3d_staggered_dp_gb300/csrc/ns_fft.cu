@@ -293,6 +293,93 @@ __global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_yz_kernel(FftPlan
   }
 }
 
+// The y transform of a packed-x box (two real lines, .x and .y, per complex
+// slot) through an FFT (Makhoul).  DCT-II of a real line x of N points
+// (dense_pair's pbc-3 matrix F[k][s] = cos(pi k (2s+1) / (2N))) is
+//   X_k = Re(exp(-i pi k / (2N)) V_k),  V = DFT_N(v),  v_m = x_{2m}, v_{N-1-m} = x_{2m+1}.
+// The two real lines of a slot share one complex FFT and are separated in the
+// post-twiddle: with U_k = exp(-i pi k / (2N)) V_k / 2 (and V_N = V_0),
+//   X_k = (Re U_k - Im U_{N-k}) + i (Im U_k + Re U_{N-k}).
+// pbc 2's matrix is the same transform of the line with its even (0-based)
+// samples negated, modes reversed (k -> N-1-k).  The inverse is the exact
+// inverse (DCT-III with its 1/N): V_k = exp(i pi k / (2N)) (X_k - i X_{N-k}) / N
+// (X_N = 0), v = the unnormalised inverse DFT of V, x_{2m} = v_m,
+// x_{2m+1} = v_{N-1-m}.  About 2.8 log2(N) / 2 + 3 FP64 instructions per real
+// value against 3N/8 + 1.5 for the folded dense products.
+template <int N, bool FWD, int PB>
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) dct_y_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
+  using F = YZ<N>;
+  constexpr int LPC = F::LPC, R1 = F::R1, R2 = F::R2, T = F::T, KQ = F::KQ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* sb = reinterpret_cast<double2*>(smem_raw);
+  const int l = threadIdx.x, t = threadIdx.y;
+  const int tl = blockIdx.x * LPC + l;
+  const bool valid = tl < P.nxs * P.nz;
+  const int col = valid ? tl % P.nxs : 0, o = valid ? tl / P.nxs : 0;
+  const long long st = P.nxs;
+  double2* g = spec + col + (long long)P.nxs * P.ny * o;
+  const double2* tw = P.dct_tw;
+  auto src_of = [](int n) { return n < N / 2 ? 2 * n : 2 * (N - 1 - n) + 1; };  // the sample v_n holds
+  auto mode_of = [](int k) { return PB == 2 ? N - 1 - k : k; };
+  auto neg = [](double2 v) { return make_double2(-v.x, -v.y); };
+  if (FWD) {
+    double2 x[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) {
+      const int s = src_of(t + R1 * n2);
+      double2 v = valid ? g[(long long)s * st] : make_double2(0.0, 0.0);
+      if (PB == 2 && (s & 1) == 0) v = neg(v);
+      x[n2] = v;
+    }
+    dft<R2, -1>(x, c);
+    sb[F::sidx(t, 0, l)] = x[0];
+#pragma unroll
+    for (int k2 = 1; k2 < R2; ++k2) sb[F::sidx(t, k2, l)] = cmul(c, x[k2], __ldg(tw + ((t * k2) % N)));
+    __syncthreads();
+    double2 xk[KQ][R1];
+    F::fwdB(xk, sb, l, t, c);  // xk[q][k1] = V[k2 + R2 k1], k2 = t + T q
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) sb[(t + T * q + R2 * k1) * LPC + l] = xk[q][k1];
+    __syncthreads();
+    if (valid)
+      for (int k = t; k <= N / 2; k += R1) {
+        const double2 Uk = cmul(c, sb[k * LPC + l], __ldg(P.dct_wf + k));
+        const double2 Um = cmul(c, sb[((N - k) % N) * LPC + l], __ldg(P.dct_wf + (N - k)));
+        g[(long long)mode_of(k) * st] = make_double2(fsub(c, Uk.x, Um.y), fadd(c, Uk.y, Um.x));
+        if (k != 0 && k != N / 2)
+          g[(long long)mode_of(N - k) * st] = make_double2(fsub(c, Um.x, Uk.y), fadd(c, Um.y, Uk.x));
+      }
+  } else {
+    double2 xk[KQ][R1];
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) {
+        const int k = t + T * q + R2 * k1;
+        const double2 X = valid ? g[(long long)mode_of(k) * st] : make_double2(0.0, 0.0);
+        const double2 Xm = (valid && k != 0) ? g[(long long)mode_of(N - k) * st] : make_double2(0.0, 0.0);
+        const double2 d = make_double2(fadd(c, X.x, Xm.y), fsub(c, X.y, Xm.x));  // X_k - i X_{N-k}
+        xk[q][k1] = cmul(c, d, __ldg(P.dct_wi + k));
+      }
+    F::invA(xk, sb, tw, l, t, c);
+    __syncthreads();
+    double2 x[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) x[k2] = sb[F::sidx(t, k2, l)];
+    dft<R2, 1>(x, c);
+#pragma unroll
+    for (int b = 0; b < R2; ++b) {
+      const int s = src_of(t + R1 * b);
+      double2 v = x[b];
+      if (PB == 2 && (s & 1) == 0) v = neg(v);
+      if (valid) g[(long long)s * st] = v;
+    }
+  }
+}
+
 template <int N>
 __global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) fft_z_solve_kernel(FftPlan P, double2* __restrict__ spec, FOne c) {
   using F = YZ<N>;
@@ -510,6 +597,19 @@ size_t xp_smem() { return (size_t)XP<M>::LINES * XP<M>::LS * sizeof(double2); }
 template <int N>
 size_t yz_smem() { return (size_t)N * lpc<N>() * sizeof(double2); }
 
+template <int N, bool FWD, int PB>
+cudaError_t launch_dct_y_n(const FftPlan& P, double2* spec, cudaStream_t st) {
+  const size_t sm = yz_smem<N>();
+  auto kern = dct_y_kernel<N, FWD, PB>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  constexpr int LPC = lpc<N>();
+  const int grid = (P.nxs * P.nz + LPC - 1) / LPC;
+  kern<<<grid, dim3(LPC, Split<N>::R1), sm, st>>>(P, spec, FOne{1.0, -0.0});
+  return cudaGetLastError();
+}
+
+
 template <int M>
 cudaError_t launch_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st) {
   const size_t sm = xp_smem<M>();
@@ -573,6 +673,17 @@ cudaError_t launch_z(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
   }
 
 }  // namespace
+
+cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t st) {
+  if (P.dct_y != 2 && P.dct_y != 3) return cudaErrorInvalidValue;
+#define DCT_Y(n)                                                                                  \
+  e = fwd ? (P.dct_y == 2 ? launch_dct_y_n<(n), true, 2>(P, spec, st) : launch_dct_y_n<(n), true, 3>(P, spec, st))  \
+          : (P.dct_y == 2 ? launch_dct_y_n<(n), false, 2>(P, spec, st) : launch_dct_y_n<(n), false, 3>(P, spec, st));
+  cudaError_t e = cudaSuccess;
+  NS_SIZE_SWITCH(P.ny, DCT_Y)
+#undef DCT_Y
+  return e;
+}
 
 bool fft_size_supported(int nx, int ny, int nz) {
   auto ok = [](int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512; };
@@ -638,6 +749,9 @@ cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec
     }
     if (e != cudaSuccess) return e;
     mk(m == 1 ? "fft_y_fwd" : "fft_z_fwd");
+  } else if (m == 1 && P.dct_y) {
+    if ((e = launch_dct_y(true, P, spec, st)) != cudaSuccess) return e;
+    mk("dct_y_fwd");
   } else {
     if ((e = launch_dense_yz(m, true, P, spec, st)) != cudaSuccess) return e;
     mk(m == 1 ? "dense_y_fwd" : "dense_z_fwd");
@@ -686,6 +800,9 @@ cudaError_t launch_poisson_inv_mid(const FftPlan& P, const DivArgs& d, double2* 
     }
     if (e != cudaSuccess) return e;
     mk(m == 1 ? "fft_y_inv" : "fft_z_inv");
+  } else if (m == 1 && P.dct_y) {
+    if ((e = launch_dct_y(false, P, spec, st)) != cudaSuccess) return e;
+    mk("dct_y_inv");
   } else {
     if ((e = launch_dense_yz(m, false, P, spec, st)) != cudaSuccess) return e;
     mk(m == 1 ? "dense_y_inv" : "dense_z_inv");

@@ -222,6 +222,12 @@ struct FftPlan {
   const double* fwd[3];   // dense forward matrices (x: F^T [n][k]; y, z: F [k][n])
   const double* inv[3];   // dense inverse matrices (x: G^T [k][n]; y, z: G [n][k])
   int sym[3];             // bit 0: F[k][N-1-n] = (-1)^k F[k][n]; bit 1: G[N-1-n][k] = (-1)^k G[n][k]
+  // A dense y axis of power-of-two length 32..512 with pbc 2 or 3 transformed through an FFT
+  // (Makhoul) instead of the dense products (session plans; ns_fft.cu dct_y_kernel):
+  int dct_y;              // 0: dense products; 2 or 3: the pressure code of the FFT-based transform
+  const double2* dct_tw;  // exp(-2 pi i m / ny), m < ny
+  const double2* dct_wf;  // exp(-i pi k / (2 ny)) / 2, k = 0..ny (forward post-twiddle)
+  const double2* dct_wi;  // exp(+i pi k / (2 ny)) / ny, k < ny (inverse pre-twiddle)
   int has_mean;           // 1: the singular mode is set to mean_val (after the forward passes)
   double mean_val;        // FFT z solve: the singular entry; tridiagonal solve: the singular line's mean
   const double* mean_dev; // non-null: the line mean is mean_val * (*mean_dev) (a mean_dp set on the device)
@@ -274,6 +280,8 @@ struct FftPlan {
   }
 };
 using SpecPlan = FftPlan;
+// The FFT-based y transform of a packed-x plan with dct_y set (ns_fft.cu).
+cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t st);
 struct DivArgs {
   Layout L;
   const double* us;
