@@ -806,6 +806,26 @@ int build_plans(ns_handle* h) {
       tw.push_back(make_double2((double)(cosl(th) / ny), (double)(sinl(th) / ny)));
     }
   }
+  // The same for a wall x axis (NS_DENSE_X keeps the dense products).
+  P.dct_x = 0;
+  size_t o_xtw = 0, o_xwf = 0, o_xwi = 0;
+  if (P.kind[0] == 1 && (c.pbc[0] == 2 || c.pbc[0] == 3) && nx >= 32 && nx <= 512 && (nx & (nx - 1)) == 0 &&
+      !std::getenv("NS_DENSE_X")) {
+    P.dct_x = c.pbc[0];
+    const long double pi = 3.141592653589793238462643383279502884L;
+    o_xtw = tw.size();
+    twid(nx, nx, tw);
+    o_xwf = tw.size();
+    for (int k = 0; k <= nx; ++k) {
+      const long double th = pi * (long double)k / (2.0L * nx);
+      tw.push_back(make_double2((double)(cosl(th) / 2.0L), (double)(-sinl(th) / 2.0L)));
+    }
+    o_xwi = tw.size();
+    for (int k = 0; k < nx; ++k) {
+      const long double th = pi * (long double)k / (2.0L * nx);
+      tw.push_back(make_double2((double)(cosl(th) / nx), (double)(sinl(th) / nx)));
+    }
+  }
   if (tw.empty()) tw.push_back(make_double2(1.0, 0.0));
   NS_CUDA(h, cudaMalloc(&h->tw, tw.size() * sizeof(double2)));
   NS_CUDA(h, cudaMemcpyAsync(h->tw, tw.data(), tw.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream));
@@ -906,6 +926,9 @@ int build_plans(ns_handle* h) {
   P.dct_tw = P.dct_y ? h->tw + o_dtw : nullptr;
   P.dct_wf = P.dct_y ? h->tw + o_dwf : nullptr;
   P.dct_wi = P.dct_y ? h->tw + o_dwi : nullptr;
+  P.dctx_tw = P.dct_x ? h->tw + o_xtw : nullptr;
+  P.dctx_wf = P.dct_x ? h->tw + o_xwf : nullptr;
+  P.dctx_wi = P.dct_x ? h->tw + o_xwi : nullptr;
   const bool zcyc = !sax && allper && c.poisson_z == 0;
   P.inv_lam = (sax || zcyc) ? nullptr : t0 + o_il;
   P.eig_x = (sax || zcyc) ? t0 + o_ex : nullptr;

@@ -685,6 +685,189 @@ cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t
   return e;
 }
 
+// The x transform of a wall x axis through the same FFT-based DCT: two real
+// x lines (rows 2l and 2l+1 of a CTA's 2 LPC rows, row = (j-1) + ny (k-1))
+// are the real and imaginary parts of one complex line.  Both passes stage
+// the rows in shared memory as pairs, pr[l (N+1) + n] = (row 2l, row 2l+1) at
+// sample or mode n (stride N+1 keeps the per-pair reads conflict-free), so
+// the global side moves whole rows with coalesced accesses.  A packed
+// spectrum row read as doubles is the modes in order.
+// The divergence (plus the pressure-BC terms) of the rows, one thread per
+// point, into out[N row + i]: a streaming pass at full occupancy, so the
+// transform below reads whole rows instead of six shifted velocity loads.
+template <int N>
+__global__ void __launch_bounds__(256) dct_x_div_kernel(FftPlan P, DivArgs d, double* __restrict__ out, FOne c) {
+  const long long idx = blockIdx.x * 256LL + threadIdx.x;
+  if (idx >= (long long)N * P.ny * P.nz) return;
+  const int i = (int)(idx % N), row = (int)(idx / N);
+  const int j = 1 + row % P.ny, k = 1 + row / P.ny;
+  const Layout& L = d.L;
+  const long long g = L.at(i + 1, j, k);
+  double v = fmul(c, fsub(c, d.us[g + 1], d.us[g]), d.cdx);
+  v = fma(fsub(c, d.vs[g + L.sy], d.vs[g]), d.cdy, v);
+  v = fma(fsub(c, d.ws[g + L.sz], d.ws[g]), d.cdz, v);
+  out[idx] = v + P.bc_term(i + 1, j, k);
+}
+
+// In place: the real rows spec_d[N row + i] (row = (j-1) + ny (k-1)) become
+// their packed modes.
+template <int N, int PB>
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) dct_x_fwd_kernel(FftPlan P, double2* spec, FOne c) {
+  using F = YZ<N>;
+  constexpr int LPC = F::LPC, R1 = F::R1, R2 = F::R2, T = F::T, KQ = F::KQ, PS = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* sb = reinterpret_cast<double2*>(smem_raw);
+  double2* pr = sb + N * LPC;
+  double* prd = reinterpret_cast<double*>(pr);
+  const int l = threadIdx.x, t = threadIdx.y;
+  const int nrows = P.ny * P.nz;
+  const int row0 = blockIdx.x * 2 * LPC;
+  const int tid = t * LPC + l, nth = LPC * R1;
+  double* out = reinterpret_cast<double*>(spec);
+  for (int e = tid; e < 2 * LPC * N; e += nth) {
+    const int rr = e / N, i = e % N, row = row0 + rr;
+    prd[2 * PS * (rr >> 1) + 2 * i + (rr & 1)] = row < nrows ? out[(long long)N * row + i] : 0.0;
+  }
+  __syncthreads();
+  auto src_of = [](int n) { return n < N / 2 ? 2 * n : 2 * (N - 1 - n) + 1; };
+  auto mode_of = [](int k) { return PB == 2 ? N - 1 - k : k; };
+  const double2* tw = P.dctx_tw;
+  {
+    double2 x[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) {
+      const int s = src_of(t + R1 * n2);
+      double2 v = pr[l * PS + s];
+      if (PB == 2 && (s & 1) == 0) v = make_double2(-v.x, -v.y);
+      x[n2] = v;
+    }
+    dft<R2, -1>(x, c);
+    sb[F::sidx(t, 0, l)] = x[0];
+#pragma unroll
+    for (int k2 = 1; k2 < R2; ++k2) sb[F::sidx(t, k2, l)] = cmul(c, x[k2], __ldg(tw + ((t * k2) % N)));
+  }
+  __syncthreads();
+  double2 xk[KQ][R1];
+  F::fwdB(xk, sb, l, t, c);
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) sb[(t + T * q + R2 * k1) * LPC + l] = xk[q][k1];
+  __syncthreads();
+  for (int k = t; k <= N / 2; k += R1) {
+    const double2 Uk = cmul(c, sb[k * LPC + l], __ldg(P.dctx_wf + k));
+    const double2 Um = cmul(c, sb[((N - k) % N) * LPC + l], __ldg(P.dctx_wf + (N - k)));
+    pr[l * PS + mode_of(k)] = make_double2(fsub(c, Uk.x, Um.y), fadd(c, Uk.y, Um.x));
+    if (k != 0 && k != N / 2) pr[l * PS + mode_of(N - k)] = make_double2(fsub(c, Um.x, Uk.y), fadd(c, Um.y, Uk.x));
+  }
+  __syncthreads();
+  for (int e = tid; e < 2 * LPC * N; e += nth) {
+    const int rr = e / N, i = e % N, row = row0 + rr;
+    if (row < nrows) out[(long long)N * row + i] = prd[2 * PS * (rr >> 1) + 2 * i + (rr & 1)];
+  }
+}
+
+template <int N, int PB>
+__global__ void __launch_bounds__(lpc<N>() * Split<N>::R1) dct_x_inv_kernel(FftPlan P, const double2* __restrict__ spec,
+                                                                            double* dp, Layout L, FOne c) {
+  using F = YZ<N>;
+  constexpr int LPC = F::LPC, R1 = F::R1, R2 = F::R2, T = F::T, KQ = F::KQ, PS = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* sb = reinterpret_cast<double2*>(smem_raw);
+  double2* pr = sb + N * LPC;
+  double* prd = reinterpret_cast<double*>(pr);
+  const int l = threadIdx.x, t = threadIdx.y;
+  const int nrows = P.ny * P.nz;
+  const int row0 = blockIdx.x * 2 * LPC;
+  const int tid = t * LPC + l, nth = LPC * R1;
+  const double* in = reinterpret_cast<const double*>(spec);
+  for (int e = tid; e < 2 * LPC * N; e += nth) {
+    const int rr = e / N, i = e % N, row = row0 + rr;
+    prd[2 * PS * (rr >> 1) + 2 * i + (rr & 1)] = row < nrows ? in[(long long)N * row + i] : 0.0;
+  }
+  __syncthreads();
+  auto src_of = [](int n) { return n < N / 2 ? 2 * n : 2 * (N - 1 - n) + 1; };
+  auto mode_of = [](int k) { return PB == 2 ? N - 1 - k : k; };
+  double2 xk[KQ][R1];
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) {
+      const int k = t + T * q + R2 * k1;
+      const double2 X = pr[l * PS + mode_of(k)];
+      const double2 Xm = k ? pr[l * PS + mode_of(N - k)] : make_double2(0.0, 0.0);
+      const double2 dd = make_double2(fadd(c, X.x, Xm.y), fsub(c, X.y, Xm.x));  // X_k - i X_{N-k}
+      xk[q][k1] = cmul(c, dd, __ldg(P.dctx_wi + k));
+    }
+  F::invA(xk, sb, P.dctx_tw, l, t, c);
+  __syncthreads();
+  {
+    double2 x[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) x[k2] = sb[F::sidx(t, k2, l)];
+    dft<R2, 1>(x, c);
+#pragma unroll
+    for (int b = 0; b < R2; ++b) {
+      const int s = src_of(t + R1 * b);
+      double2 v = x[b];
+      if (PB == 2 && (s & 1) == 0) v = make_double2(-v.x, -v.y);
+      pr[l * PS + s] = v;
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < 2 * LPC * N; e += nth) {
+    const int rr = e / N, i = e % N, row = row0 + rr;
+    if (row < nrows) dp[L.at(i + 1, 1 + row % P.ny, 1 + row / P.ny)] = prd[2 * PS * (rr >> 1) + 2 * i + (rr & 1)];
+  }
+}
+
+template <int N, int PB>
+cudaError_t launch_dct_x_n(bool fwd, const FftPlan& P, const DivArgs* d, double2* spec, const double2* cspec,
+                           double* dp, const Layout& L, cudaStream_t st, const Marker* mk) {
+  constexpr int LPC = lpc<N>();
+  const size_t sm = yz_smem<N>() + (size_t)LPC * (N + 1) * sizeof(double2);
+  const int grid = (P.ny * P.nz + 2 * LPC - 1) / (2 * LPC);
+  const FOne c{1.0, -0.0};
+  cudaError_t e;
+  if (fwd) {
+    const long long pts = (long long)N * P.ny * P.nz;
+    dct_x_div_kernel<N><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(P, *d, reinterpret_cast<double*>(spec), c);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (mk) (*mk)("dct_x_div");
+    e = cudaFuncSetAttribute(dct_x_fwd_kernel<N, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dct_x_fwd_kernel<N, PB><<<grid, dim3(LPC, Split<N>::R1), sm, st>>>(P, spec, c);
+  } else {
+    e = cudaFuncSetAttribute(dct_x_inv_kernel<N, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    dct_x_inv_kernel<N, PB><<<grid, dim3(LPC, Split<N>::R1), sm, st>>>(P, cspec, dp, L, c);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dct_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st, const Marker& mk) {
+  if ((P.dct_x != 2 && P.dct_x != 3) || d.rhs) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+#define DCT_XF(n)                                                                                   \
+  e = P.dct_x == 2 ? launch_dct_x_n<(n), 2>(true, P, &d, spec, nullptr, nullptr, d.L, st, &mk)      \
+                   : launch_dct_x_n<(n), 3>(true, P, &d, spec, nullptr, nullptr, d.L, st, &mk);
+  NS_SIZE_SWITCH(P.nx, DCT_XF)
+#undef DCT_XF
+  return e;
+}
+
+cudaError_t launch_dct_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, cudaStream_t st) {
+  if (P.dct_x != 2 && P.dct_x != 3) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+#define DCT_XI(n)                                                                                   \
+  e = P.dct_x == 2 ? launch_dct_x_n<(n), 2>(false, P, nullptr, nullptr, spec, dp, L, st, nullptr)   \
+                   : launch_dct_x_n<(n), 3>(false, P, nullptr, nullptr, spec, dp, L, st, nullptr);
+  NS_SIZE_SWITCH(P.nx, DCT_XI)
+#undef DCT_XI
+  return e;
+}
+
 bool fft_size_supported(int nx, int ny, int nz) {
   auto ok = [](int n) { return n == 16 || n == 32 || n == 64 || n == 128 || n == 256 || n == 512; };
   return ok(nx) && ok(ny) && ok(nz);
@@ -729,6 +912,9 @@ cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec
 #undef X_FWD
     if (e != cudaSuccess) return e;
     mk("fft_x_fwd");
+  } else if (P.dct_x && !d.rhs) {
+    if ((e = launch_dct_x_fwd(P, d, spec, st, mk)) != cudaSuccess) return e;
+    mk("dct_x_fwd");
   } else {
     if ((e = launch_dense_x(true, P, d, spec, dp, L, st)) != cudaSuccess) return e;
     mk("dense_x_fwd");
@@ -825,6 +1011,9 @@ cudaError_t launch_poisson_inv_x(const FftPlan& P, const DivArgs& d, double2* sp
 #undef X_INV
     if (e != cudaSuccess) return e;
     mk("fft_x_inv");
+  } else if (P.dct_x) {
+    if ((e = launch_dct_x_inv(P, spec, dp, L, st)) != cudaSuccess) return e;
+    mk("dct_x_inv");
   } else {
     if ((e = launch_dense_x(false, P, d, spec, dp, L, st)) != cudaSuccess) return e;
     mk("dense_x_inv");

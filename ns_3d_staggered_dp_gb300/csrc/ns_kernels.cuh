@@ -228,6 +228,11 @@ struct FftPlan {
   const double2* dct_tw;  // exp(-2 pi i m / ny), m < ny
   const double2* dct_wf;  // exp(-i pi k / (2 ny)) / 2, k = 0..ny (forward post-twiddle)
   const double2* dct_wi;  // exp(+i pi k / (2 ny)) / ny, k < ny (inverse pre-twiddle)
+  // The same for a wall x axis (packed modes; two x lines per complex FFT):
+  int dct_x;
+  const double2* dctx_tw;  // exp(-2 pi i m / nx), m < nx
+  const double2* dctx_wf;  // exp(-i pi k / (2 nx)) / 2, k = 0..nx
+  const double2* dctx_wi;  // exp(+i pi k / (2 nx)) / nx, k < nx
   int has_mean;           // 1: the singular mode is set to mean_val (after the forward passes)
   double mean_val;        // FFT z solve: the singular entry; tridiagonal solve: the singular line's mean
   const double* mean_dev; // non-null: the line mean is mean_val * (*mean_dev) (a mean_dp set on the device)
@@ -258,7 +263,14 @@ struct FftPlan {
   const double* face_hi[3];
 
   // pr_bc_staggered_modify_rhs (NS_functions.f90:1345-1400) at interior cell (i, j, k).
+  // Interior cells leave through one integer test: the boundary terms sit in
+  // a call so that they are branched around, not predicated (a predicated-off
+  // FP64 instruction still takes its FP64-pipe issue slot at every cell).
   __device__ __forceinline__ double bc_term(int i, int j, int k) const {
+    if (i != 1 && i != nx && j != 1 && j != ny && k != 1 && k != nz) return 0.0;
+    return bc_term_edge(i, j, k);
+  }
+  __device__ __noinline__ double bc_term_edge(int i, int j, int k) const {
     double t = 0.0;
     const int n[3] = {nx, ny, nz};
     const int idx[3] = {i, j, k};
@@ -282,6 +294,11 @@ struct FftPlan {
 using SpecPlan = FftPlan;
 // The FFT-based y transform of a packed-x plan with dct_y set (ns_fft.cu).
 cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t st);
+struct DivArgs;
+// The FFT-based x transforms of a plan with dct_x set (ns_fft.cu): divergence
+// (+ pressure-BC terms) -> packed modes, and packed modes -> dp slots 1..nx.
+cudaError_t launch_dct_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st, const Marker& mk);
+cudaError_t launch_dct_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, cudaStream_t st);
 struct DivArgs {
   Layout L;
   const double* us;

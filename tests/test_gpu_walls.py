@@ -64,6 +64,10 @@ POISSON_CASES = [
     ((16, 200, 16), (3, 3, 3)),
     ((16, 512, 16), (1, 2, 3)),
     ((1024, 16, 16), (3, 3, 3)),
+    # FFT-based DCT x passes (power-of-two nx, codes 2 and 3) at their size limits
+    ((512, 16, 24), (2, 3, 3)),
+    ((128, 32, 16), (3, 2, 2)),
+    ((256, 12, 10), (2, 4, 3)),
 ]
 
 
