@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -387,11 +388,14 @@ struct ns_batch {
   // work items: per active set (0 regular, s >= 1 sub-step s of the first
   // interval), per stage: offset, count, and per-subdomain ranges
   BatchItem* d_items = nullptr;
-  struct Range { long long off = 0; int cnt = 0; };
+  // cnt_dense: the leading items of a spectral stage that take the dense
+  // kernel (the rest take the FFT-based one); cnt for every other stage
+  struct Range { long long off = 0; int cnt = 0; int cnt_dense = 0; };
   std::vector<std::vector<Range>> rng;                  // [set][stage]
   std::vector<std::vector<std::vector<Range>>> sub_rng; // [set][stage][sub]
   std::vector<std::vector<int>> active;                 // [set] -> subdomains
   size_t spec_smem[5] = {0, 0, 0, 0, 0};
+  size_t spec_smem_dct[4] = {0, 0, 0, 0};
   // gather / capture items (all subdomains)
   Range gather_rng, capture_rng;
   // state
@@ -472,7 +476,15 @@ cudaError_t launch_stage_kernel(ns_batch* b, int set, int stage, bool first, cud
         break;
       case ST_XF: case ST_YF: case ST_TRI: case ST_YI: case ST_XI: {
         const int pass = pass_of[stage - ST_XF];
-        e = launch_spec_batch(pass, b->d_spec[v], p, cnt, b->spec_smem[pass], want > 0 ? grid : 0, st);
+        const int nd = r.cnt_dense, nf = cnt - r.cnt_dense;
+        if (nd > 0)
+          e = launch_spec_batch(pass, false, b->d_spec[v], p, nd, b->spec_smem[pass],
+                                want > 0 ? persistent_grid(want, nd) : 0, st);
+        if (e == cudaSuccess && nf > 0) {
+          if (nd > 0) ++b->launches;
+          e = launch_spec_batch(pass, true, b->d_spec[v], p + nd, nf, b->spec_smem_dct[pass],
+                                want > 0 ? persistent_grid(want, nf) : 0, st);
+        }
         break;
       }
       case ST_CORRECT:
@@ -715,6 +727,36 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   std::vector<double> tab;
   std::map<int, size_t> xF, xG, yF, yG, ex, ey;
   std::map<int, int> ysym, xsym;  // symmetry bits of the y and x pairs per size
+  // FFT-based DCT tables of the power-of-two axes of 32 and 64 points (pressure
+  // codes 2 and 3; NS_DENSE_X / NS_DENSE_Y keep the dense products): the
+  // N-point twiddles exp(-2 pi i m / N), m < N, then exp(-i pi k / (2N)) / 2,
+  // k <= N, then exp(i pi k / (2N)) / N, k < N, as (re, im) pairs.
+  std::map<int, size_t> dtab;
+  const bool dct_code = c.pbc == 2 || c.pbc == 3;
+  auto dct_size = [](int m) { return m == 32 || m == 64; };
+  auto add_dct = [&](int N) {
+    if (dtab.count(N)) return;
+    dtab[N] = tab.size();
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int m = 0; m < N; ++m) {
+      const long double th = 2.0L * pi * (long double)m / (long double)N;
+      tab.push_back((double)cosl(th)); tab.push_back((double)(-sinl(th)));
+    }
+    for (int k = 0; k <= N; ++k) {
+      const long double th = pi * (long double)k / (2.0L * N);
+      tab.push_back((double)(cosl(th) / 2.0L)); tab.push_back((double)(-sinl(th) / 2.0L));
+    }
+    for (int k = 0; k < N; ++k) {
+      const long double th = pi * (long double)k / (2.0L * N);
+      tab.push_back((double)(cosl(th) / N)); tab.push_back((double)(sinl(th) / N));
+    }
+    tab.resize(align32(tab.size()));
+  };
+  const bool dct_x_on = dct_code && !std::getenv("NS_DENSE_X"), dct_y_on = dct_code && !std::getenv("NS_DENSE_Y");
+  for (int i = 0; i < n; ++i) {
+    if (dct_x_on && dct_size(subs[i].nx)) add_dct(subs[i].nx);
+    if (dct_y_on && dct_size(subs[i].ny)) add_dct(subs[i].ny);
+  }
   for (int i = 0; i < n; ++i) {
     const int nx = subs[i].nx, ny = subs[i].ny;
     if (!xF.count(nx)) {
@@ -834,6 +876,16 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     S.sym[0] = xsym[d.nx];
     S.eig_x = b->tables + ex[d.nx];
     S.eig_o = b->tables + ey[d.ny];
+    if (dct_x_on && dct_size(d.nx)) {
+      const double2* t2 = reinterpret_cast<const double2*>(b->tables + dtab[d.nx]);
+      S.dct_x = c.pbc;
+      S.dctx_tw = t2; S.dctx_wf = t2 + d.nx; S.dctx_wi = t2 + 2 * d.nx + 1;
+    }
+    if (dct_y_on && dct_size(d.ny)) {
+      const double2* t2 = reinterpret_cast<const double2*>(b->tables + dtab[d.ny]);
+      S.dct_y = c.pbc;
+      S.dct_tw = t2; S.dct_wf = t2 + d.ny; S.dct_wi = t2 + 2 * d.ny + 1;
+    }
     S.tri_h2 = c.dz * c.dz;
     S.tri_rs = c.dz * c.dz;
     S.tri_elo = S.tri_ehi = c.pbc == 2 ? -1.0 : (c.pbc == 3 ? 1.0 : 0.0);
@@ -894,7 +946,10 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     }
   }
   for (int pass = 0; pass < 5; ++pass)
-    for (int i = 0; i < n; ++i) b->spec_smem[pass] = std::max(b->spec_smem[pass], spec_pass_smem(pass, b->plan[i]));
+    for (int i = 0; i < n; ++i) {
+      size_t& sm = spec_pass_dct(pass, b->plan[i]) ? b->spec_smem_dct[pass] : b->spec_smem[pass];
+      sm = std::max(sm, spec_pass_smem(pass, b->plan[i]));
+    }
 
   // ---- work items ----
   auto chunks = [](long long e) { return (int)((e + kChunk - 1) / kChunk); };
@@ -949,14 +1004,26 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
       if (set == 0 || subs[i].sub_tstep >= set) b->active[set].push_back(i);
   b->rng.assign(nsets, std::vector<ns_batch::Range>(ST_COUNT));
   b->sub_rng.assign(nsets, std::vector<std::vector<ns_batch::Range>>(ST_COUNT, std::vector<ns_batch::Range>(n)));
+  // A spectral stage lists the subdomains of its dense kernel first, then
+  // those of its FFT-based kernel.
+  auto stage_dct = [&](int st, int i) {
+    const int pass_of[5] = {0, 2, 4, 3, 1};
+    return st >= ST_XF && st <= ST_XI && spec_pass_dct(pass_of[st - ST_XF], b->plan[i]);
+  };
   for (int set = 0; set < nsets; ++set)
     for (int st = 0; st < ST_COUNT; ++st) {
       b->rng[set][st].off = (long long)all.size();
-      for (int i : b->active[set]) {
-        std::vector<BatchItem> v = sub_items(i, st, set);
-        b->sub_rng[set][st][i].off = (long long)all.size();
-        b->sub_rng[set][st][i].cnt = (int)v.size();
-        all.insert(all.end(), v.begin(), v.end());
+      for (int group = 0; group < 2; ++group) {
+        for (int i : b->active[set]) {
+          const bool dct = stage_dct(st, i);
+          if ((int)dct != group) continue;
+          std::vector<BatchItem> v = sub_items(i, st, set);
+          b->sub_rng[set][st][i].off = (long long)all.size();
+          b->sub_rng[set][st][i].cnt = (int)v.size();
+          b->sub_rng[set][st][i].cnt_dense = dct ? 0 : (int)v.size();
+          all.insert(all.end(), v.begin(), v.end());
+        }
+        if (group == 0) b->rng[set][st].cnt_dense = (int)((long long)all.size() - b->rng[set][st].off);
       }
       b->rng[set][st].cnt = (int)((long long)all.size() - b->rng[set][st].off);
     }

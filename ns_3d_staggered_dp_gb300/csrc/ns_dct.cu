@@ -27,6 +27,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ns_fft_core.cuh"
 #include "ns_internal.cuh"
 #include "ns_kernels.cuh"
 
@@ -674,7 +675,37 @@ __device__ __forceinline__ void tri_lines_body(const SpecPlan& S, double2* __res
 // Batched passes: persistent CTAs walk (subdomain, block) work items; the
 // subdomain's arguments are staged in shared memory once per item.
 // PASS: 0 x forward, 1 x inverse, 2 y forward, 3 y inverse, 4 tridiagonal z (packed x).
+// A subdomain whose plan sets dct_x / dct_y (a power-of-two axis of 32 or 64
+// points, pressure code 2 or 3) takes the FFT-based line bodies of
+// ns_fft_core.cuh there, with 128 / R1 lines per item so that all 128
+// threads work; the others take the dense products.
 // ---------------------------------------------------------------------------
+__host__ __device__ constexpr int batch_dct_lpc(int n) { return 128 / (n == 64 ? Split<64>::R1 : Split<32>::R1); }
+
+template <int N, int PB>
+__device__ __forceinline__ void batch_dct(int pass, const BatchSpecArgs& a, double2* sb, int bx) {
+  constexpr int LPC = batch_dct_lpc(N);
+  const FOne c{a.d.one, a.d.mzero};
+  const int l = threadIdx.x % LPC, t = threadIdx.x / LPC;
+  if (pass == 0) dct_x_fwd_body<N, PB, true, LPC>(a.S, &a.d, a.spec, sb, bx, l, t, c);
+  else if (pass == 1) dct_x_inv_body<N, PB, LPC>(a.S, a.spec, a.dp, a.L, sb, bx, l, t, c);
+  else if (pass == 2) dct_y_body<N, true, PB, LPC>(a.S, a.spec, sb, bx, l, t, c);
+  else dct_y_body<N, false, PB, LPC>(a.S, a.spec, sb, bx, l, t, c);
+}
+
+template <int PASS>
+__device__ __forceinline__ void batch_dct_dispatch(const BatchSpecArgs& a, double2* sb, int bx) {
+  const int n = PASS < 2 ? a.S.nx : a.S.ny;
+  const int pb = PASS < 2 ? a.S.dct_x : a.S.dct_y;
+  if (n == 64) {
+    if (pb == 2) batch_dct<64, 2>(PASS, a, sb, bx);
+    else batch_dct<64, 3>(PASS, a, sb, bx);
+  } else {
+    if (pb == 2) batch_dct<32, 2>(PASS, a, sb, bx);
+    else batch_dct<32, 3>(PASS, a, sb, bx);
+  }
+}
+
 template <int PASS>
 __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __restrict__ tab,
                                                          const BatchItem* __restrict__ items, int n_items) {
@@ -693,10 +724,27 @@ __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __
   }
 }
 
+template <int PASS>
+__global__ void __launch_bounds__(128) spec_batch_dct_kernel(const BatchSpecArgs* __restrict__ tab,
+                                                             const BatchItem* __restrict__ items, int n_items) {
+  extern __shared__ __align__(16) double2 sm_d[];
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    batch_dct_dispatch<PASS>(tab[w.sub], sm_d, w.bx);
+    __syncthreads();
+  }
+}
+
+bool spec_pass_dct(int pass, const SpecPlan& S) {
+  return ((pass == 0 || pass == 1) && S.dct_x) || ((pass == 2 || pass == 3) && S.dct_y);
+}
+
 // Work-item grid of one pass for one subdomain.
 void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
   gy = 1;
-  if (pass == 0 || pass == 1) {
+  if ((pass == 0 || pass == 1) && S.dct_x) gx = (S.ny * S.nz + 2 * batch_dct_lpc(S.nx) - 1) / (2 * batch_dct_lpc(S.nx));
+  else if ((pass == 2 || pass == 3) && S.dct_y) gx = (S.nxs * S.nz + batch_dct_lpc(S.ny) - 1) / batch_dct_lpc(S.ny);
+  else if (pass == 0 || pass == 1) {
     const int per = 128 / (pass == 0 ? dense_x_group(S.nx) : dense_x_inv_group(S.sym[0], S.nx));
     gx = (S.ny * S.nz + per - 1) / per;
   }
@@ -705,16 +753,26 @@ void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
 }
 
 size_t spec_pass_smem(int pass, const SpecPlan& S) {
+  if ((pass == 0 || pass == 1) && S.dct_x) {
+    const size_t L = batch_dct_lpc(S.nx);
+    return (size_t)S.nx * L * sizeof(double2) + L * (S.nx + 1) * sizeof(double2);
+  }
+  if ((pass == 2 || pass == 3) && S.dct_y) return (size_t)S.ny * batch_dct_lpc(S.ny) * sizeof(double2);
   if (pass == 0) return (size_t)(128 / dense_x_group(S.nx)) * S.nx * sizeof(double);
   if (pass == 1) return (size_t)(128 / dense_x_inv_group(S.sym[0], S.nx)) * S.nx * sizeof(double);
   if (pass == 2 || pass == 3) return (size_t)S.ny * 16 * sizeof(double2);
   return (size_t)S.nz * TRI_T * sizeof(double) * 2;
 }
 
-cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchItem* items, int n_items, size_t smem,
-                              int grid, cudaStream_t st) {
+cudaError_t launch_spec_batch(int pass, bool dct, const BatchSpecArgs* tab, const BatchItem* items, int n_items,
+                              size_t smem, int grid, cudaStream_t st) {
   if (n_items <= 0) return cudaSuccess;
-  auto kern = pass == 0 ? spec_batch_kernel<0>
+  if (dct && (pass < 0 || pass > 3)) return cudaErrorInvalidValue;
+  auto kern = dct ? (pass == 0 ? spec_batch_dct_kernel<0>
+                   : pass == 1 ? spec_batch_dct_kernel<1>
+                   : pass == 2 ? spec_batch_dct_kernel<2>
+                               : spec_batch_dct_kernel<3>)
+            : pass == 0 ? spec_batch_kernel<0>
             : pass == 1 ? spec_batch_kernel<1>
             : pass == 2 ? spec_batch_kernel<2>
             : pass == 3 ? spec_batch_kernel<3>

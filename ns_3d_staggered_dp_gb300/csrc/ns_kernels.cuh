@@ -370,10 +370,14 @@ struct BatchSpecArgs {
   Layout L;
 };
 // pass: 0 x forward (divergence + BC terms), 1 x inverse, 2 y forward, 3 y inverse, 4 z line solve.
+// A subdomain takes the FFT-based kernel of passes 0-3 where spec_pass_dct
+// says so (its plan's dct_x / dct_y), the dense kernel otherwise; the two
+// kernels take separate item lists (their register needs differ).
+bool spec_pass_dct(int pass, const SpecPlan& S);
 void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy);
 size_t spec_pass_smem(int pass, const SpecPlan& S);
-cudaError_t launch_spec_batch(int pass, const BatchSpecArgs* tab, const BatchItem* items, int n_items, size_t smem,
-                              int grid, cudaStream_t st);
+cudaError_t launch_spec_batch(int pass, bool dct, const BatchSpecArgs* tab, const BatchItem* items, int n_items,
+                              size_t smem, int grid, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)

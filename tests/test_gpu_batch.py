@@ -104,6 +104,18 @@ def test_batch_matches_oracle(restart):
         _compare(g, r)
 
 
+# x and y edges of 32 and 64 take the FFT-based DCT passes (codes 2 and 3),
+# beside a 16-wide box on the dense products in the same launch sequence
+DCT_SUBS = [(1, 1, 1, 32, 64, 16, 1), (3, 2, 5, 64, 32, 24, 2), (7, 1, 2, 16, 32, 16, 1)]
+
+
+@pytest.mark.parametrize("pbc", [3, 2])
+def test_batch_fft_dct_sizes(pbc):
+    got, refs, _ = run_case(DCT_SUBS, False, n_intervals=3, pbc=pbc)
+    for g, r in zip(got, refs):
+        _compare(g, r)
+
+
 @pytest.mark.parametrize("bc,pbc", [(2, 2), (4, 4)])
 def test_batch_wall_codes(bc, pbc):
     got, refs, _ = run_case(SUBS[:2], False, n_intervals=3, bc=bc, pbc=pbc)
@@ -111,9 +123,10 @@ def test_batch_wall_codes(bc, pbc):
         _compare(g, r)
 
 
-def test_batch_loop_mode_is_bitwise_identical():
-    a, _, la = run_case(SUBS, False, n_intervals=3, mode=0)
-    b, _, lb = run_case(SUBS, False, n_intervals=3, mode=1)
+@pytest.mark.parametrize("subs", [SUBS, DCT_SUBS])
+def test_batch_loop_mode_is_bitwise_identical(subs):
+    a, _, la = run_case(subs, False, n_intervals=3, mode=0)
+    b, _, lb = run_case(subs, False, n_intervals=3, mode=1)
     for x, y in zip(a, b):
         for k in ("u", "v", "w", "p", "hx", "hy", "hz"):
             assert np.array_equal(x[k], y[k]), k
