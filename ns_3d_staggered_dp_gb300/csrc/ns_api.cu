@@ -784,13 +784,14 @@ int build_plans(ns_handle* h) {
   if (P.kind[1] == 0) twid(ny, ny, tw);
   o_z = tw.size();
   if (P.kind[2] == 0) twid(nz, nz, tw);
-  // A dense y (in front of a wall z) of power-of-two length >= 32 with pbc 2
-  // or 3 goes through an FFT: its twiddles and the DCT pre/post-twiddles.
-  // (NS_DENSE_Y in the environment keeps the dense products, for comparison.)
+  // A dense y (in front of a wall z) of length 24, 48 or a power of two from
+  // 32 to 512 with pbc 2 or 3 goes through an FFT: its twiddles and the DCT
+  // pre/post-twiddles.  (NS_DENSE_Y in the environment keeps the dense
+  // products, for comparison.)
+  auto dct_len = [](int m) { return m == 24 || m == 48 || (m >= 32 && m <= 512 && (m & (m - 1)) == 0); };
   P.dct_y = 0;
   size_t o_dtw = 0, o_dwf = 0, o_dwi = 0;
-  if (P.kind[1] == 1 && (c.pbc[1] == 2 || c.pbc[1] == 3) && ny >= 32 && ny <= 512 &&
-      (ny & (ny - 1)) == 0 && !std::getenv("NS_DENSE_Y")) {
+  if (P.kind[1] == 1 && (c.pbc[1] == 2 || c.pbc[1] == 3) && dct_len(ny) && !std::getenv("NS_DENSE_Y")) {
     P.dct_y = c.pbc[1];
     const long double pi = 3.141592653589793238462643383279502884L;
     o_dtw = tw.size();
@@ -809,8 +810,7 @@ int build_plans(ns_handle* h) {
   // The same for a wall x axis (NS_DENSE_X keeps the dense products).
   P.dct_x = 0;
   size_t o_xtw = 0, o_xwf = 0, o_xwi = 0;
-  if (P.kind[0] == 1 && (c.pbc[0] == 2 || c.pbc[0] == 3) && nx >= 32 && nx <= 512 && (nx & (nx - 1)) == 0 &&
-      !std::getenv("NS_DENSE_X")) {
+  if (P.kind[0] == 1 && (c.pbc[0] == 2 || c.pbc[0] == 3) && dct_len(nx) && !std::getenv("NS_DENSE_X")) {
     P.dct_x = c.pbc[0];
     const long double pi = 3.141592653589793238462643383279502884L;
     o_xtw = tw.size();

@@ -393,6 +393,9 @@ struct ns_batch {
   struct Range { long long off = 0; int cnt = 0; int cnt_dense = 0; };
   std::vector<std::vector<Range>> rng;                  // [set][stage]
   std::vector<std::vector<std::vector<Range>>> sub_rng; // [set][stage][sub]
+  // the divergence items of the x forward stage (subdomains with an FFT-based x)
+  std::vector<Range> div_rng;                           // [set]
+  std::vector<std::vector<Range>> sub_div_rng;          // [set][sub]
   std::vector<std::vector<int>> active;                 // [set] -> subdomains
   size_t spec_smem[5] = {0, 0, 0, 0, 0};
   size_t spec_smem_dct[4] = {0, 0, 0, 0};
@@ -477,6 +480,14 @@ cudaError_t launch_stage_kernel(ns_batch* b, int set, int stage, bool first, cud
       case ST_XF: case ST_YF: case ST_TRI: case ST_YI: case ST_XI: {
         const int pass = pass_of[stage - ST_XF];
         const int nd = r.cnt_dense, nf = cnt - r.cnt_dense;
+        if (stage == ST_XF) {
+          const ns_batch::Range& dr = loop ? b->sub_div_rng[set][act[k]] : b->div_rng[set];
+          if (dr.cnt > 0) {
+            e = launch_spec_batch_div(b->d_spec[v], b->d_items + dr.off, dr.cnt, 0, st);
+            if (e != cudaSuccess) return e;
+            ++b->launches;
+          }
+        }
         if (nd > 0)
           e = launch_spec_batch(pass, false, b->d_spec[v], p, nd, b->spec_smem[pass],
                                 want > 0 ? persistent_grid(want, nd) : 0, st);
@@ -632,6 +643,29 @@ int ns_batch_destroy(ns_batch* b) {
   return NS_OK;
 }
 
+// The tables of an FFT-based DCT line of N points as (re, im) pairs: the
+// N-point twiddles exp(-2 pi i m / N), m < N, the forward post-twiddles
+// exp(-i pi k / (2N)) / 2, k <= N, and the inverse pre-twiddles
+// exp(i pi k / (2N)) / N, k < N; computed in long double.
+static void append_dct_tables(int N, std::vector<double>& tab) {
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int m = 0; m < N; ++m) {
+    const long double th = 2.0L * pi * (long double)m / (long double)N;
+    tab.push_back((double)cosl(th));
+    tab.push_back((double)(-sinl(th)));
+  }
+  for (int k = 0; k <= N; ++k) {
+    const long double th = pi * (long double)k / (2.0L * N);
+    tab.push_back((double)(cosl(th) / 2.0L));
+    tab.push_back((double)(-sinl(th) / 2.0L));
+  }
+  for (int k = 0; k < N; ++k) {
+    const long double th = pi * (long double)k / (2.0L * N);
+    tab.push_back((double)(cosl(th) / N));
+    tab.push_back((double)(sinl(th) / N));
+  }
+}
+
 int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n, ns_batch** out) {
   if (!cfg || !subs || n <= 0 || !out) return NS_ERR_ARG;
   *out = nullptr;
@@ -727,29 +761,17 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
   std::vector<double> tab;
   std::map<int, size_t> xF, xG, yF, yG, ex, ey;
   std::map<int, int> ysym, xsym;  // symmetry bits of the y and x pairs per size
-  // FFT-based DCT tables of the power-of-two axes of 32 and 64 points (pressure
+  // FFT-based DCT tables of the axes of 24, 32, 48 and 64 points (pressure
   // codes 2 and 3; NS_DENSE_X / NS_DENSE_Y keep the dense products): the
   // N-point twiddles exp(-2 pi i m / N), m < N, then exp(-i pi k / (2N)) / 2,
   // k <= N, then exp(i pi k / (2N)) / N, k < N, as (re, im) pairs.
   std::map<int, size_t> dtab;
   const bool dct_code = c.pbc == 2 || c.pbc == 3;
-  auto dct_size = [](int m) { return m == 32 || m == 64; };
+  auto dct_size = [](int m) { return m == 24 || m == 32 || m == 48 || m == 64; };
   auto add_dct = [&](int N) {
     if (dtab.count(N)) return;
     dtab[N] = tab.size();
-    const long double pi = 3.141592653589793238462643383279502884L;
-    for (int m = 0; m < N; ++m) {
-      const long double th = 2.0L * pi * (long double)m / (long double)N;
-      tab.push_back((double)cosl(th)); tab.push_back((double)(-sinl(th)));
-    }
-    for (int k = 0; k <= N; ++k) {
-      const long double th = pi * (long double)k / (2.0L * N);
-      tab.push_back((double)(cosl(th) / 2.0L)); tab.push_back((double)(-sinl(th) / 2.0L));
-    }
-    for (int k = 0; k < N; ++k) {
-      const long double th = pi * (long double)k / (2.0L * N);
-      tab.push_back((double)(cosl(th) / N)); tab.push_back((double)(sinl(th) / N));
-    }
+    append_dct_tables(N, tab);
     tab.resize(align32(tab.size()));
   };
   const bool dct_x_on = dct_code && !std::getenv("NS_DENSE_X"), dct_y_on = dct_code && !std::getenv("NS_DENSE_Y");
@@ -1027,6 +1049,21 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
       }
       b->rng[set][st].cnt = (int)((long long)all.size() - b->rng[set][st].off);
     }
+  b->div_rng.assign(nsets, ns_batch::Range{});
+  b->sub_div_rng.assign(nsets, std::vector<ns_batch::Range>(n));
+  for (int set = 0; set < nsets; ++set) {
+    b->div_rng[set].off = (long long)all.size();
+    for (int i : b->active[set]) {
+      if (!stage_dct(ST_XF, i)) continue;
+      const Layout& L = b->L[i];
+      const long long ne = (long long)L.nx * L.ny * L.nz;
+      const int nq = (int)((ne + kDivChunk - 1) / kDivChunk);
+      b->sub_div_rng[set][i].off = (long long)all.size();
+      b->sub_div_rng[set][i].cnt = nq;
+      for (int q = 0; q < nq; ++q) all.push_back(BatchItem{i, q, 0, 0});
+    }
+    b->div_rng[set].cnt = (int)((long long)all.size() - b->div_rng[set].off);
+  }
   b->gather_rng.off = (long long)all.size();
   for (int i = 0; i < n; ++i) {
     std::vector<BatchItem> v = sub_items(i, ST_CORRECT, 0);

@@ -675,19 +675,21 @@ __device__ __forceinline__ void tri_lines_body(const SpecPlan& S, double2* __res
 // Batched passes: persistent CTAs walk (subdomain, block) work items; the
 // subdomain's arguments are staged in shared memory once per item.
 // PASS: 0 x forward, 1 x inverse, 2 y forward, 3 y inverse, 4 tridiagonal z (packed x).
-// A subdomain whose plan sets dct_x / dct_y (a power-of-two axis of 32 or 64
+// A subdomain whose plan sets dct_x / dct_y (an axis of 24, 32, 48 or 64
 // points, pressure code 2 or 3) takes the FFT-based line bodies of
 // ns_fft_core.cuh there, with 128 / R1 lines per item so that all 128
 // threads work; the others take the dense products.
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int batch_dct_lpc(int n) { return 128 / (n == 64 ? Split<64>::R1 : Split<32>::R1); }
+__host__ __device__ constexpr int batch_dct_lpc(int n) {
+  return 128 / (n == 64 ? Split<64>::R1 : n == 48 ? Split<48>::R1 : n == 32 ? Split<32>::R1 : Split<24>::R1);
+}
 
 template <int N, int PB>
 __device__ __forceinline__ void batch_dct(int pass, const BatchSpecArgs& a, double2* sb, int bx) {
   constexpr int LPC = batch_dct_lpc(N);
   const FOne c{a.d.one, a.d.mzero};
   const int l = threadIdx.x % LPC, t = threadIdx.x / LPC;
-  if (pass == 0) dct_x_fwd_body<N, PB, true, LPC>(a.S, &a.d, a.spec, sb, bx, l, t, c);
+  if (pass == 0) dct_x_fwd_body<N, PB, false, LPC>(a.S, nullptr, a.spec, sb, bx, l, t, c);
   else if (pass == 1) dct_x_inv_body<N, PB, LPC>(a.S, a.spec, a.dp, a.L, sb, bx, l, t, c);
   else if (pass == 2) dct_y_body<N, true, PB, LPC>(a.S, a.spec, sb, bx, l, t, c);
   else dct_y_body<N, false, PB, LPC>(a.S, a.spec, sb, bx, l, t, c);
@@ -700,9 +702,15 @@ __device__ __forceinline__ void batch_dct_dispatch(const BatchSpecArgs& a, doubl
   if (n == 64) {
     if (pb == 2) batch_dct<64, 2>(PASS, a, sb, bx);
     else batch_dct<64, 3>(PASS, a, sb, bx);
-  } else {
+  } else if (n == 48) {
+    if (pb == 2) batch_dct<48, 2>(PASS, a, sb, bx);
+    else batch_dct<48, 3>(PASS, a, sb, bx);
+  } else if (n == 32) {
     if (pb == 2) batch_dct<32, 2>(PASS, a, sb, bx);
     else batch_dct<32, 3>(PASS, a, sb, bx);
+  } else {
+    if (pb == 2) batch_dct<24, 2>(PASS, a, sb, bx);
+    else batch_dct<24, 3>(PASS, a, sb, bx);
   }
 }
 
@@ -733,6 +741,36 @@ __global__ void __launch_bounds__(128) spec_batch_dct_kernel(const BatchSpecArgs
     batch_dct_dispatch<PASS>(tab[w.sub], sm_d, w.bx);
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(kDivChunk) spec_batch_div_kernel(const BatchSpecArgs* __restrict__ tab,
+                                                                   const BatchItem* __restrict__ items, int n_items) {
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    const BatchSpecArgs& a = tab[w.sub];
+    const int N = a.S.nx;
+    const long long e = (long long)w.bx * kDivChunk + threadIdx.x;
+    if (e < (long long)N * a.S.ny * a.S.nz) {
+      const int i = (int)(e % N), row = (int)(e / N);
+      const FOne c{a.d.one, a.d.mzero};
+      reinterpret_cast<double*>(a.spec)[e] = rhs_cell(a.d, a.S, c, i + 1, 1 + row % a.S.ny, 1 + row / a.S.ny);
+    }
+  }
+}
+
+cudaError_t launch_spec_batch_div(const BatchSpecArgs* tab, const BatchItem* items, int n_items, int grid,
+                                  cudaStream_t st) {
+  if (n_items <= 0) return cudaSuccess;
+  if (grid <= 0) {
+    int per_sm = 0, dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spec_batch_div_kernel, kDivChunk, 0);
+    grid = (per_sm > 0 ? per_sm : 1) * nsm;
+  }
+  if (grid > n_items) grid = n_items;
+  spec_batch_div_kernel<<<grid, kDivChunk, 0, st>>>(tab, items, n_items);
+  return cudaGetLastError();
 }
 
 bool spec_pass_dct(int pass, const SpecPlan& S) {

@@ -394,6 +394,20 @@ cudaError_t launch_z(const FftPlan& P, double2* spec, FOne c, cudaStream_t st) {
     default: return cudaErrorInvalidValue; \
   }
 
+// The lengths of the FFT-based DCT passes: 24 and 48 (one 12-point stage)
+// and the powers of two from 32 to 512.
+#define NS_DCT_SIZE_SWITCH(n, CALL) \
+  switch (n) {                      \
+    case 24: CALL(24); break;       \
+    case 32: CALL(32); break;       \
+    case 48: CALL(48); break;       \
+    case 64: CALL(64); break;       \
+    case 128: CALL(128); break;     \
+    case 256: CALL(256); break;     \
+    case 512: CALL(512); break;     \
+    default: return cudaErrorInvalidValue; \
+  }
+
 }  // namespace
 
 cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t st) {
@@ -402,7 +416,7 @@ cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t
   e = fwd ? (P.dct_y == 2 ? launch_dct_y_n<(n), true, 2>(P, spec, st) : launch_dct_y_n<(n), true, 3>(P, spec, st))  \
           : (P.dct_y == 2 ? launch_dct_y_n<(n), false, 2>(P, spec, st) : launch_dct_y_n<(n), false, 3>(P, spec, st));
   cudaError_t e = cudaSuccess;
-  NS_SIZE_SWITCH(P.ny, DCT_Y)
+  NS_DCT_SIZE_SWITCH(P.ny, DCT_Y)
 #undef DCT_Y
   return e;
 }
@@ -470,7 +484,7 @@ cudaError_t launch_dct_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, 
 #define DCT_XF(n)                                                                                   \
   e = P.dct_x == 2 ? launch_dct_x_n<(n), 2>(true, P, &d, spec, nullptr, nullptr, d.L, st, &mk)      \
                    : launch_dct_x_n<(n), 3>(true, P, &d, spec, nullptr, nullptr, d.L, st, &mk);
-  NS_SIZE_SWITCH(P.nx, DCT_XF)
+  NS_DCT_SIZE_SWITCH(P.nx, DCT_XF)
 #undef DCT_XF
   return e;
 }
@@ -481,7 +495,7 @@ cudaError_t launch_dct_x_inv(const FftPlan& P, const double2* spec, double* dp, 
 #define DCT_XI(n)                                                                                   \
   e = P.dct_x == 2 ? launch_dct_x_n<(n), 2>(false, P, nullptr, nullptr, spec, dp, L, st, nullptr)   \
                    : launch_dct_x_n<(n), 3>(false, P, nullptr, nullptr, spec, dp, L, st, nullptr);
-  NS_SIZE_SWITCH(P.nx, DCT_XI)
+  NS_DCT_SIZE_SWITCH(P.nx, DCT_XI)
 #undef DCT_XI
   return e;
 }

@@ -87,7 +87,7 @@ __device__ __forceinline__ void bfly(double2& a, double2& b, int q, const FOne& 
   b.x = fma(-f, y.x, a0.x); b.y = fma(-f, y.y, a0.y);
 }
 
-// In-place R-point DFT (R a power of two, R <= 32), natural order in and out.
+// Radix-2 in-place R-point DFT (R a power of two, R <= 32), natural order in and out.
 // Every index is a template constant, so the array stays in registers.
 template <int R, int I>
 struct BitRev {
@@ -121,9 +121,56 @@ struct Stage {
   }
 };
 template <int R, int DIR>
-__device__ __forceinline__ void dft(double2 (&x)[R], const FOne& c) {
+__device__ __forceinline__ void dft_pow2(double2 (&x)[R], const FOne& c) {
   BitRev<R, 0>::run(x);
   Stage<R, 2, DIR>::run(x, c);
+}
+
+// 3-point DFT in FMA form: with s = a1 + a2, d = a1 - a2 and t = a0 - s/2,
+// X0 = a0 + s, X1 = t - i (sqrt(3)/2) d, X2 = t + i (sqrt(3)/2) d (forward;
+// the inverse takes the conjugate roots).
+template <int DIR>
+__device__ __forceinline__ void dft3(double2& a0, double2& a1, double2& a2, const FOne& c) {
+  constexpr double H3 = 0.86602540378443864676;  // sqrt(3)/2
+  const double2 s = make_double2(fadd(c, a1.x, a2.x), fadd(c, a1.y, a2.y));
+  const double2 d = make_double2(fsub(c, a1.x, a2.x), fsub(c, a1.y, a2.y));
+  const double2 t = make_double2(fma(s.x, -0.5, a0.x), fma(s.y, -0.5, a0.y));
+  a0 = make_double2(fadd(c, a0.x, s.x), fadd(c, a0.y, s.y));
+  const double g = DIR < 0 ? H3 : -H3;
+  a1 = make_double2(fma(g, d.y, t.x), fma(-g, d.x, t.y));
+  a2 = make_double2(fma(-g, d.y, t.x), fma(g, d.x, t.y));
+}
+
+// 12-point DFT by the prime-factor (Good-Thomas) split 12 = 3 x 4, which
+// needs no twiddles: 3-point DFTs over n1 of x[(4 n1 + 3 n2) mod 12] for each
+// n2, then 4-point DFTs over n2, whose output k2 of row k1 is
+// X[(4 k1 + 9 k2) mod 12] (9 = 3 x (3^-1 mod 4), 4 = 4 x (4^-1 mod 3)).
+template <int DIR>
+__device__ __forceinline__ void dft12(double2 (&x)[12], const FOne& c) {
+  double2 y[4][3];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    double2 a0 = x[(3 * n2) % 12], a1 = x[(4 + 3 * n2) % 12], a2 = x[(8 + 3 * n2) % 12];
+    dft3<DIR>(a0, a1, a2, c);
+    y[n2][0] = a0;
+    y[n2][1] = a1;
+    y[n2][2] = a2;
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    double2 z[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft_pow2<4, DIR>(z, c);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) x[(4 * k1 + 9 * k2) % 12] = z[k2];
+  }
+}
+
+// In-place R-point DFT, natural order in and out: R a power of two up to 32,
+// or 12.
+template <int R, int DIR>
+__device__ __forceinline__ void dft(double2 (&x)[R], const FOne& c) {
+  if constexpr (R == 12) dft12<DIR>(x, c);
+  else dft_pow2<R, DIR>(x, c);
 }
 
 __device__ __forceinline__ double2 cmul(const FOne& c, double2 a, double2 w) {
@@ -142,6 +189,8 @@ __device__ __forceinline__ double2 cmulc(const FOne& c, double2 a, double2 w) { 
 // Four-step split N = R1 * R2 (R1 <= R2), T = R1 threads per line.
 template <int N> struct Split;
 template <> struct Split<8> { static constexpr int R1 = 2, R2 = 4; };
+template <> struct Split<24> { static constexpr int R1 = 2, R2 = 12; };
+template <> struct Split<48> { static constexpr int R1 = 4, R2 = 12; };
 template <> struct Split<16> { static constexpr int R1 = 4, R2 = 4; };
 template <> struct Split<32> { static constexpr int R1 = 4, R2 = 8; };
 template <> struct Split<64> { static constexpr int R1 = 8, R2 = 8; };

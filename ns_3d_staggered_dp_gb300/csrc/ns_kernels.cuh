@@ -378,6 +378,14 @@ void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy);
 size_t spec_pass_smem(int pass, const SpecPlan& S);
 cudaError_t launch_spec_batch(int pass, bool dct, const BatchSpecArgs* tab, const BatchItem* items, int n_items,
                               size_t smem, int grid, cudaStream_t st);
+// The divergence rows (plus the pressure-BC terms) of the subdomains whose x
+// forward pass is FFT-based, into their spectrum buffers as rows of nx
+// doubles (row = (j-1) + ny (k-1)); item (sub, q) covers the elements
+// [kDivChunk q, kDivChunk (q+1)).  The FFT-based x forward then transforms
+// the rows in place.
+constexpr int kDivChunk = 256;
+cudaError_t launch_spec_batch_div(const BatchSpecArgs* tab, const BatchItem* items, int n_items, int grid,
+                                  cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)

@@ -104,9 +104,10 @@ def test_batch_matches_oracle(restart):
         _compare(g, r)
 
 
-# x and y edges of 32 and 64 take the FFT-based DCT passes (codes 2 and 3),
+# x and y edges of 24, 32, 48 and 64 take the FFT-based DCT passes (codes 2 and 3),
 # beside a 16-wide box on the dense products in the same launch sequence
-DCT_SUBS = [(1, 1, 1, 32, 64, 16, 1), (3, 2, 5, 64, 32, 24, 2), (7, 1, 2, 16, 32, 16, 1)]
+DCT_SUBS = [(1, 1, 1, 32, 64, 16, 1), (3, 2, 5, 64, 32, 24, 2), (7, 1, 2, 16, 32, 16, 1), (2, 3, 1, 48, 24, 16, 1),
+            (1, 2, 3, 24, 48, 32, 4)]
 
 
 @pytest.mark.parametrize("pbc", [3, 2])
