@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(kChunk) capture_kernel(const SubGeo* __restric
       }
       e = r;
     }
-    const int n1 = plane_n1(L, a);
-    const int s1 = (int)(e % n1), s2 = (int)(e / n1);
+    const unsigned n1 = (unsigned)plane_n1(L, a);
+    const int s2 = (int)((unsigned)e / n1), s1 = (int)((unsigned)e - (unsigned)s2 * n1);  // e < one face plane
     const int a1 = a == 0 ? 1 : 0, a2 = a == 2 ? 1 : 2;
     const int n3[3] = {L.nx, L.ny, L.nz};
     // reference (0-based) indices along a1, a2

@@ -55,12 +55,15 @@ __device__ __forceinline__ void correct_body(const CorrectArgs& a, int i, int j,
   }
 }
 
-// Flat slot index t of the padded box (x fastest).
-__device__ __forceinline__ void correct_body(const CorrectArgs& a, long long t) {
+// Flat slot index t of the padded box (x fastest).  A subdomain box holds
+// fewer than 2^31 slots, so the split takes two 32-bit divisions (a 64-bit
+// division by a runtime value is a long software sequence per slot).
+__device__ __forceinline__ void correct_body(const CorrectArgs& a, unsigned t) {
   const Layout L = a.L;
-  const int nx2 = L.nx + 2, ny2 = L.ny + 2, nz2 = L.nz + 2;
-  if (t >= (long long)nx2 * ny2 * nz2) return;
-  correct_body(a, (int)(t % nx2), (int)((t / nx2) % ny2), (int)(t / ((long long)nx2 * ny2)));
+  const unsigned nx2 = (unsigned)L.nx + 2u, ny2 = (unsigned)L.ny + 2u, nz2 = (unsigned)L.nz + 2u;
+  if (t >= nx2 * ny2 * nz2) return;
+  const unsigned r = t / nx2, k = r / ny2;
+  correct_body(a, (int)(t - r * nx2), (int)(r - k * ny2), (int)k);
 }
 
 // Plane k0 + blockIdx.y; the x blocks cover its (nx+2)(ny+2) slots, which a
@@ -78,7 +81,7 @@ __global__ void __launch_bounds__(256) correct_batch_kernel(const CorrectArgs* _
                                                             const BatchItem* __restrict__ items, int n_items) {
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const BatchItem w = items[it];
-    correct_body(tab[w.sub], (long long)w.bx * 256 + threadIdx.x);
+    correct_body(tab[w.sub], (unsigned)w.bx * 256u + threadIdx.x);
   }
 }
 

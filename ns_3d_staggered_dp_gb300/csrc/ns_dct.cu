@@ -748,10 +748,10 @@ __global__ void __launch_bounds__(kDivChunk) spec_batch_div_kernel(const BatchSp
   for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
     const BatchItem w = items[it];
     const BatchSpecArgs& a = tab[w.sub];
-    const int N = a.S.nx;
-    const long long e = (long long)w.bx * kDivChunk + threadIdx.x;
-    if (e < (long long)N * a.S.ny * a.S.nz) {
-      const int i = (int)(e % N), row = (int)(e / N);
+    const unsigned N = (unsigned)a.S.nx;
+    const unsigned e = (unsigned)w.bx * kDivChunk + threadIdx.x;  // a subdomain box holds < 2^31 cells
+    if (e < N * (unsigned)a.S.ny * (unsigned)a.S.nz) {
+      const int row = (int)(e / N), i = (int)(e - (unsigned)row * N);
       const FOne c{a.d.one, a.d.mzero};
       reinterpret_cast<double*>(a.spec)[e] = rhs_cell(a.d, a.S, c, i + 1, 1 + row % a.S.ny, 1 + row / a.S.ny);
     }
