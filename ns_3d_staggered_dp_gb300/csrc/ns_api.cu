@@ -956,22 +956,22 @@ int build_plans(ns_handle* h) {
     NS_CUDA(h, launch_cyc_table(P, h->cyc_buf, h->stream));
     NS_CUDA(h, cudaStreamSynchronize(h->stream));
   }
-  // The wall-axis line solve computes its multipliers: with a warp per 32
-  // lines and 32 warps per SM the division chain is hidden, and a table
-  // (the batched solve's choice, launch_tri_table) only adds a second load
-  // stream (256x128x256 y solve: 0.28 ms computed, 0.37 ms from a table).
-  // A packed-x (all-wall) box's z solve keeps two multipliers per line in
-  // shared memory, 2 nz x 32 doubles a warp, which at nz = 256 leaves one
-  // warp per SM: it reads them from a table instead (same bits).
+  // The wall-axis line solve: the twisted factorisation from a table of its
+  // multipliers made once here (no division in the solve, two lanes per
+  // line).  The one-lane Thomas solve that computes its multipliers stays
+  // for lines shorter than 8 (NS_TRI_THOMAS keeps it, for comparison).
   P.tri_m = nullptr;
   P.sing_cm = nullptr;
-  if (sax == 2 && P.kind[0] == 1) {
+  P.tri_tw = 0;
+  const int nsax = sax == 1 ? ny : nz;
+  if (sax != 0 && nsax >= 8 && !std::getenv("NS_TRI_THOMAS")) {
     NS_CUDA(h, cudaMalloc(&h->tri_tab, (size_t)nxs * ny * nz * sizeof(double2)));
-    NS_CUDA(h, cudaMalloc(&h->sing_cm, (size_t)2 * nz * 32 * sizeof(double)));
-    NS_CUDA(h, launch_tri_table(2, P, h->tri_tab, h->stream));
+    NS_CUDA(h, cudaMalloc(&h->sing_cm, (size_t)2 * nsax * 32 * sizeof(double)));
+    NS_CUDA(h, launch_tri_twist_table(sax, P, h->tri_tab, h->stream));
     NS_CUDA(h, cudaStreamSynchronize(h->stream));
     P.tri_m = h->tri_tab;
     P.sing_cm = h->sing_cm;
+    P.tri_tw = 1;
   }
   return NS_OK;
 }

@@ -914,8 +914,9 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
     S.has_mean = c.pbc == 3 ? 1 : 0;
     S.mean_val = (double)d.nx * (double)d.ny;
     S.mean_dev = g.mean;
-    if (launch_tri_table(2, S, b->tri_tab + tri_off[i], b->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
+    if (launch_tri_twist_table(2, S, b->tri_tab + tri_off[i], b->stream) != cudaSuccess) return bail(NS_ERR_CUDA);
     S.tri_m = b->tri_tab + tri_off[i];
+    S.tri_tw = 1;
     for (int a = 0; a < 3; ++a) {
       const double hh = hs[a];
       if (c.pbc == 2) { S.mod_lo[a] = -2.0 / (hh * hh); S.mod_hi[a] = -2.0 / (hh * hh); }

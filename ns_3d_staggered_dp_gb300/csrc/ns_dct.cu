@@ -416,11 +416,12 @@ __device__ __forceinline__ void dense_yz_body(const SpecPlan& S, double2* __rest
 // sigma = lambda_x + lambda_other, e_j the pressure-BC change of the end rows.
 // Its solution is that of the per-axis transform, eigenvalue divide and
 // inverse transform of DCT_poisson_solver (NS_functions.f90:1505-1630) along s.
-// One thread per line (Thomas, no pivoting: the rows are diagonally
-// dominant); the multipliers go to shared memory, the forward-eliminated rhs
-// back to the line in place.  The one singular line (Neumann/periodic
-// everywhere, both modes 0) drops its rhs mean, pins its last entry and takes
-// the mean value (NS_functions.f90:1576-1577).
+// The solve used for lines of 8 rows and more is the twisted factorisation
+// from a table of multipliers (tri_twist_body, below); this one-thread
+// Thomas solve (no pivoting: the rows are diagonally dominant) computes its
+// multipliers into shared memory and serves shorter lines.  The one singular
+// line (Neumann/periodic everywhere, both modes 0) drops its rhs mean, pins
+// its last entry and takes the mean value (NS_functions.f90:1576-1577).
 // ---------------------------------------------------------------------------
 constexpr int TRI_T = 32;  // lines per CTA (one warp)
 
@@ -457,6 +458,60 @@ __device__ void tri_real(double* x, long long sx, int N, double sig_h2, double e
     for (int j = 0; j < N; ++j) x[j * sx] += shift;
   }
 }
+
+// The singular line by a whole warp.  Its system is the Neumann one along
+// the axis (end rows -x_0 + x_1, x_{N-2} - x_{N-1}; sigma = 0), whose
+// solution with the rhs mean dropped and the mean set to target (the
+// reference pins the last entry and shifts, NS_functions.f90:1576-1577) is
+// the flux F_j = x_{j+1} - x_j = sum_{i<=j} R_i, R = rs (r - mean r), then
+// x_j = sum_{i<j} F_i shifted to the target mean: two prefix sums over the
+// warp, lane l holding the rows [l seg, l seg + seg), seg = ceil(N/32).  r is
+// read from src (stride 1, re-read by each pass), the solution written to x
+// (stride sx doubles).
+__device__ __noinline__ void sing_line_warp(const double* src, double* x, long long sx, int N, double rs,
+                                            double target) {
+  const int lane = threadIdx.x & 31;
+  const int seg = (N + 31) / 32, j0 = min(lane * seg, N), j1 = min(j0 + seg, N);
+  auto warp_sum = [](double v) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+  };
+  auto warp_excl = [&](double tot) {  // exclusive scan of the lanes' totals
+    double incl = tot;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
+    }
+    return incl - tot;
+  };
+  double s = 0.0;
+  for (int j = j0; j < j1; ++j) s += src[j];
+  const double mean_r = warp_sum(s) / N;
+  s = 0.0;
+  for (int j = j0; j < j1; ++j) s += (src[j] - mean_r) * rs;
+  const double f0 = warp_excl(s);  // F before this lane's rows
+  // x_j = x_{j0} + sum_{j0<=i<j} F_i: the lane's sum of F over its rows
+  double fs = 0.0, f = f0;
+  for (int j = j0; j < j1; ++j) {
+    f += (src[j] - mean_r) * rs;
+    fs += f;
+  }
+  const double xb = warp_excl(fs);  // x at this lane's first row (x_0 = 0)
+  double xv = xb, ms = 0.0;
+  f = f0;
+  for (int j = j0; j < j1; ++j) {
+    x[(long long)j * sx] = xv;
+    ms += xv;
+    f += (src[j] - mean_r) * rs;
+    xv += f;
+  }
+  const double shift = target - warp_sum(ms) / N;
+  __syncwarp();
+  for (int j = j0; j < j1; ++j) x[(long long)j * sx] += shift;
+}
+
 
 template <int AXIS, bool PACKED>
 __device__ __forceinline__ void tri_solve_body(const SpecPlan& S, double2* __restrict__ spec, double* cm, int bx,
@@ -537,47 +592,6 @@ __global__ void __launch_bounds__(128) dense_yz_kernel(SpecPlan S, double2* __re
   extern __shared__ __align__(16) double2 ls_yz[];
   dense_yz_body<AXIS, FWD>(S, spec, ls_yz, blockIdx.x);
 }
-// The forward multipliers of tri_solve_body's lines, by its own recurrence
-// (same operations in the same order, so the same bits), into tab at the
-// spectrum index of each entry.  The singular line keeps its own path.
-template <int AXIS, bool PACKED>
-__global__ void __launch_bounds__(TRI_T) tri_table_kernel(SpecPlan S, double2* __restrict__ tab) {
-  const int l = threadIdx.x;
-  const int bx = blockIdx.x, by = blockIdx.y;
-  const int N = AXIS == 1 ? S.ny : S.nz;
-  const int n_other = AXIS == 1 ? S.nz : S.ny;
-  const int nreg = PACKED ? S.nxs : S.nxs - 1;
-  const int nblk = (nreg + TRI_T - 1) / TRI_T;
-  int col, o;
-  bool valid;
-  if (bx < nblk) {
-    col = bx * TRI_T + l;
-    o = by;
-    valid = col < nreg;
-  } else {
-    if (by * TRI_T >= n_other) return;
-    col = S.nxs - 1;
-    o = by * TRI_T + l;
-    valid = o < n_other;
-  }
-  if (!valid) return;
-  const long long st = AXIS == 1 ? (long long)S.nxs : (long long)S.nxs * S.ny;
-  double2* g = tab + (AXIS == 1 ? col + (long long)S.nxs * S.ny * o : col + (long long)S.nxs * o);
-  const double lo = __ldg(S.eig_o + o);
-  const double sr = (__ldg(S.eig_x + (PACKED ? 2 * col : col)) + lo) * S.tri_h2;
-  const double si = PACKED ? (__ldg(S.eig_x + 2 * col + 1) + lo) * S.tri_h2 : sr;
-  const double elo = S.tri_elo, ehi = S.tri_ehi;
-  double mr = 0.0, mi = 0.0;
-  for (int j = 0; j < N; ++j) {
-    double br = -2.0 + sr, bi = -2.0 + si;
-    if (j == 0) { br += elo; bi += elo; }
-    if (j == N - 1) { br += ehi; bi += ehi; }
-    mr = 1.0 / (br - mr);
-    if (PACKED) mi = 1.0 / (bi - mi);
-    else mi = mr;
-    g[(long long)j * st] = make_double2(mr, mi);
-  }
-}
 
 template <int AXIS, bool PACKED>
 __global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* __restrict__ spec) {
@@ -585,96 +599,214 @@ __global__ void __launch_bounds__(TRI_T) tri_solve_kernel(SpecPlan S, double2* _
   tri_solve_body<AXIS, PACKED>(S, spec, cm_tri, blockIdx.x, blockIdx.y);
 }
 
-// The z solve of a packed-x box with its multiplier table (S.tri_m), one
-// thread per line over the flattened (x column, y mode) index t = col + nxs*o:
-// full warps whatever nxs is, and no shared memory but the singular line's
-// scratch (cm, thread 0 of block 0).  Same operations as tri_solve_body.
-__device__ __forceinline__ void tri_lines_body(const SpecPlan& S, double2* __restrict__ spec, double* cm, int bx) {
-  const int N = S.nz;
-  const int t = bx * blockDim.x + threadIdx.x;
-  if (t >= S.nxs * S.ny) return;
-  const long long st = (long long)S.nxs * S.ny;
-  double2* g = spec + t;
+
+// ---------------------------------------------------------------------------
+// Twisted, table-driven line solve (the session's wall axis, 1 or 2, and
+// the batch's z axis).  Line
+// t = col + nxs o (o: z for y lines, y for z lines) of N rows; k = N/2.  Its
+// table holds m_j = 1/(b_j - m_{j-1}) for j < k (top-down, as tri_solve_body),
+// n_j = 1/(b_j - n_{j+1}) for j > k (bottom-up) and the middle pivot
+// 1/(b_k - m_{k-1} - n_{k+1}).  Lanes l and l + 16 of a warp take line l:
+// the top lane forms d_j = (rs r_j - d_{j-1}) m_j downwards, the bottom lane
+// e_j = (rs r_j - e_{j+1}) n_j upwards; the middle row gives
+// x_k = (rs r_k - d_{k-1} - e_{k+1}) piv, and the lanes substitute outwards,
+// x_j = d_j - m_j x_{j+1} above and x_j = e_j - n_j x_{j-1} below.  No
+// division in the solve, twice the lines' lanes in flight and half the
+// recurrence length of the one-lane Thomas solve; the sums round
+// differently.  The singular line takes the general path on its top lane.
+// ---------------------------------------------------------------------------
+struct TwLine {
+  long long base, st;
+  int col, o;
+  bool valid;
+};
+template <int AXIS>
+__device__ __forceinline__ TwLine tw_line(const SpecPlan& S, int t) {
+  TwLine L;
+  L.valid = t < S.nxs * (AXIS == 1 ? S.nz : S.ny);
+  if (!L.valid) t = 0;
+  L.col = t % S.nxs;
+  L.o = t / S.nxs;
+  if (AXIS == 1) { L.base = L.col + (long long)S.nxs * S.ny * L.o; L.st = S.nxs; }
+  else { L.base = t; L.st = (long long)S.nxs * S.ny; }
+  return L;
+}
+
+template <int AXIS, bool PACKED>
+__global__ void __launch_bounds__(128) tri_twist_table_kernel(SpecPlan S, double2* __restrict__ tab) {
+  const TwLine ln = tw_line<AXIS>(S, blockIdx.x * 128 + threadIdx.x);
+  if (!ln.valid) return;
+  const int N = AXIS == 1 ? S.ny : S.nz, k = N / 2;
+  const double lo = __ldg(S.eig_o + ln.o);
+  const double sr = (__ldg(S.eig_x + (PACKED ? 2 * ln.col : ln.col)) + lo) * S.tri_h2;
+  const double si = PACKED ? (__ldg(S.eig_x + 2 * ln.col + 1) + lo) * S.tri_h2 : sr;
+  const double elo = S.tri_elo, ehi = S.tri_ehi;
+  auto bj = [&](int j, double s) {
+    double b = -2.0 + s;
+    if (j == 0) b += elo;
+    if (j == N - 1) b += ehi;
+    return b;
+  };
+  double2* g = tab + ln.base;
+  double mr = 0.0, mi = 0.0;
+  for (int j = 0; j < k; ++j) {
+    mr = 1.0 / (bj(j, sr) - mr);
+    mi = PACKED ? 1.0 / (bj(j, si) - mi) : mr;
+    g[(long long)j * ln.st] = make_double2(mr, mi);
+  }
+  double nr = 0.0, ni = 0.0;
+  for (int j = N - 1; j > k; --j) {
+    nr = 1.0 / (bj(j, sr) - nr);
+    ni = PACKED ? 1.0 / (bj(j, si) - ni) : nr;
+    g[(long long)j * ln.st] = make_double2(nr, ni);
+  }
+  const double pr = 1.0 / (bj(k, sr) - mr - nr);
+  const double pi = PACKED ? 1.0 / (bj(k, si) - mi - ni) : pr;
+  g[(long long)k * ln.st] = make_double2(pr, pi);
+}
+
+// One 128-thread block bx of the twisted solve (64 lines); scr: scratch of
+// 2 N TRI_T doubles for the singular line.
+template <int AXIS, bool PACKED>
+__device__ __forceinline__ void tri_twist_body(const SpecPlan& S, double2* __restrict__ spec, double* scr, int bx) {
+  constexpr int TP = 4;  // rows and multipliers loaded ahead
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, h = lane >> 4;
+  const int t0 = (bx * 4 + warp) * 16;
+  if (t0 >= S.nxs * (AXIS == 1 ? S.nz : S.ny)) return;  // the whole warp
+  const TwLine ln = tw_line<AXIS>(S, t0 + (lane & 15));
+  const int N = AXIS == 1 ? S.ny : S.nz, k = N / 2;
+  // The singular line (col 0, o 0: lane 0 of the first warp) of a Neumann
+  // axis goes to the whole warp after the other lines (sing_line_warp); its
+  // rhs is set aside in the scratch first, since the twisted lanes also run
+  // over it (a packed box's second mode of that slot is a regular line).
+  // Otherwise it takes the one-lane general path on its top lane.
+  const bool warp_sing = t0 == 0 && S.has_mean && S.tri_elo == 1.0 && S.tri_ehi == 1.0 && N <= 512;
+  const bool sing = ln.valid && S.has_mean && ln.col == 0 && ln.o == 0;
+  const bool work = ln.valid && (!sing || warp_sing);
+  if (warp_sing) {
+    const double2* g0 = spec;  // line (0, 0)
+    for (int j = lane; j < N; j += 32) {
+      const double2 r = g0[(long long)j * (AXIS == 1 ? (long long)S.nxs : (long long)S.nxs * S.ny)];
+      scr[j] = r.x;
+      if (!PACKED) scr[N + j] = r.y;
+    }
+    __syncwarp();
+  }
+  double2* g = spec + ln.base;
+  const double2* __restrict__ tm = S.tri_m + ln.base;
+  const long long st = ln.st;
   const double rs = S.tri_rs;
-  if (S.has_mean && t == 0) {  // the singular line (col 0, o 0): its own path
+  const int cnt = h ? N - 1 - k : k;
+  auto row = [&](int q) { return h ? N - 1 - q : q; };
+  const double2 z2 = make_double2(0.0, 0.0);
+  // elimination towards the middle row
+  double2 d = z2;
+  if (work) {
+    double2 rv[TP], mv[TP];
+#pragma unroll
+    for (int q = 0; q < TP; ++q) {
+      const bool in = q < cnt;
+      rv[q] = in ? g[(long long)row(q) * st] : z2;
+      mv[q] = in ? __ldg(tm + (long long)row(q) * st) : z2;
+    }
+    for (int q0 = 0; q0 < cnt; q0 += TP) {
+      double2 rn[TP], mn[TP];
+#pragma unroll
+      for (int q = 0; q < TP; ++q) {
+        const int qq = q0 + TP + q;
+        const bool in = qq < cnt;
+        rn[q] = in ? g[(long long)row(qq) * st] : z2;
+        mn[q] = in ? __ldg(tm + (long long)row(qq) * st) : z2;
+      }
+#pragma unroll
+      for (int q = 0; q < TP; ++q)
+        if (q0 + q < cnt) {
+          d.x = fma(rv[q].x, rs, -d.x) * mv[q].x;
+          d.y = fma(rv[q].y, rs, -d.y) * mv[q].y;
+          g[(long long)row(q0 + q) * st] = d;
+        }
+#pragma unroll
+      for (int q = 0; q < TP; ++q) {
+        rv[q] = rn[q];
+        mv[q] = mn[q];
+      }
+    }
+  }
+  // the middle row, on the top lane, with the bottom lane's e_{k+1}
+  const double ex = __shfl_xor_sync(0xffffffffu, d.x, 16), ey = __shfl_xor_sync(0xffffffffu, d.y, 16);
+  double2 xk = z2;
+  if (work && h == 0) {
+    const double2 r = g[(long long)k * st];
+    const double2 pv = __ldg(tm + (long long)k * st);
+    xk.x = (fma(r.x, rs, -d.x) - ex) * pv.x;
+    xk.y = (fma(r.y, rs, -d.y) - ey) * pv.y;
+    g[(long long)k * st] = xk;
+  }
+  xk.x = __shfl_sync(0xffffffffu, xk.x, lane & 15);
+  xk.y = __shfl_sync(0xffffffffu, xk.y, lane & 15);
+  // substitution away from the middle row (row index cnt - 1 - q)
+  if (work) {
+    double2 p = xk;
+    double2 rv[TP], mv[TP];
+#pragma unroll
+    for (int q = 0; q < TP; ++q) {
+      const int qq = cnt - 1 - q;
+      const bool in = qq >= 0;
+      rv[q] = in ? g[(long long)row(qq) * st] : z2;
+      mv[q] = in ? __ldg(tm + (long long)row(qq) * st) : z2;
+    }
+    for (int q0 = 0; q0 < cnt; q0 += TP) {
+      double2 rn[TP], mn[TP];
+#pragma unroll
+      for (int q = 0; q < TP; ++q) {
+        const int qq = cnt - 1 - (q0 + TP + q);
+        const bool in = qq >= 0;
+        rn[q] = in ? g[(long long)row(qq) * st] : z2;
+        mn[q] = in ? __ldg(tm + (long long)row(qq) * st) : z2;
+      }
+#pragma unroll
+      for (int q = 0; q < TP; ++q) {
+        const int qq = cnt - 1 - (q0 + q);
+        if (qq >= 0) {
+          p.x = fma(-mv[q].x, p.x, rv[q].x);
+          p.y = fma(-mv[q].y, p.y, rv[q].y);
+          g[(long long)row(qq) * st] = p;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < TP; ++q) {
+        rv[q] = rn[q];
+        mv[q] = mn[q];
+      }
+    }
+  }
+  const double target = S.mean_dev ? S.mean_val * *S.mean_dev : S.mean_val;
+  if (warp_sing) {
+    __syncwarp();
+    const long long st0 = AXIS == 1 ? (long long)S.nxs : (long long)S.nxs * S.ny;
+    double* x0 = reinterpret_cast<double*>(spec);
+    sing_line_warp(scr, x0, 2 * st0, N, rs, target);
+    if (!PACKED) sing_line_warp(scr + N, x0 + 1, 2 * st0, N, rs, 0.0);
+  } else if (sing && h == 0) {
     const double lo = __ldg(S.eig_o);
     const double sr = (__ldg(S.eig_x) + lo) * S.tri_h2;
-    const double si = (__ldg(S.eig_x + 1) + lo) * S.tri_h2;
+    const double si = PACKED ? (__ldg(S.eig_x + 1) + lo) * S.tri_h2 : sr;
     double* x = reinterpret_cast<double*>(g);
-    tri_real(x, 2 * st, N, sr, S.tri_elo, S.tri_ehi, rs, cm, true, S.mean_dev ? S.mean_val * *S.mean_dev : S.mean_val);
-    tri_real(x + 1, 2 * st, N, si, S.tri_elo, S.tri_ehi, rs, cm + (long long)N * TRI_T, false, 0.0);
-    return;
+    tri_real(x, 2 * st, N, sr, S.tri_elo, S.tri_ehi, rs, scr, true, target);
+    tri_real(x + 1, 2 * st, N, si, S.tri_elo, S.tri_ehi, rs, scr + (long long)N * TRI_T, !PACKED, 0.0);
   }
-  // Software-pipelined in groups of TP unknowns: the next group's values and
-  // multipliers are loaded before the current group is computed and stored,
-  // so no load waits behind a store of the same line (same operations, same
-  // bits as one unknown at a time).
-  constexpr int TP = 8;
-  const double2* __restrict__ tm = S.tri_m + t;
-  double2 rv[TP], mv[TP];
-#pragma unroll
-  for (int q = 0; q < TP; ++q) {
-    const bool in = q < N;
-    rv[q] = in ? g[(long long)q * st] : make_double2(0.0, 0.0);
-    mv[q] = in ? __ldg(tm + (long long)q * st) : make_double2(0.0, 0.0);
-  }
-  double2 d = make_double2(0.0, 0.0);
-  for (int j0 = 0; j0 < N; j0 += TP) {
-    double2 rn[TP], mn[TP];
-#pragma unroll
-    for (int q = 0; q < TP; ++q) {
-      const int j = j0 + TP + q;
-      const bool in = j < N;
-      rn[q] = in ? g[(long long)j * st] : make_double2(0.0, 0.0);
-      mn[q] = in ? __ldg(tm + (long long)j * st) : make_double2(0.0, 0.0);
-    }
-#pragma unroll
-    for (int q = 0; q < TP; ++q) {
-      const int j = j0 + q;
-      if (j < N) {
-        d.x = fma(rv[q].x, rs, -d.x) * mv[q].x;
-        d.y = fma(rv[q].y, rs, -d.y) * mv[q].y;
-        g[(long long)j * st] = d;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < TP; ++q) { rv[q] = rn[q]; mv[q] = mn[q]; }
-  }
-  double2 p = d;
-#pragma unroll
-  for (int q = 0; q < TP; ++q) {
-    const int j = N - 2 - q;
-    const bool in = j >= 0;
-    rv[q] = in ? g[(long long)j * st] : make_double2(0.0, 0.0);
-    mv[q] = in ? __ldg(tm + (long long)j * st) : make_double2(0.0, 0.0);
-  }
-  for (int j0 = N - 2; j0 >= 0; j0 -= TP) {
-    double2 rn[TP], mn[TP];
-#pragma unroll
-    for (int q = 0; q < TP; ++q) {
-      const int j = j0 - TP - q;
-      const bool in = j >= 0;
-      rn[q] = in ? g[(long long)j * st] : make_double2(0.0, 0.0);
-      mn[q] = in ? __ldg(tm + (long long)j * st) : make_double2(0.0, 0.0);
-    }
-#pragma unroll
-    for (int q = 0; q < TP; ++q) {
-      const int j = j0 - q;
-      if (j >= 0) {
-        p.x = fma(-mv[q].x, p.x, rv[q].x);
-        p.y = fma(-mv[q].y, p.y, rv[q].y);
-        g[(long long)j * st] = p;
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < TP; ++q) { rv[q] = rn[q]; mv[q] = mn[q]; }
-  }
+}
+
+template <int AXIS, bool PACKED>
+__global__ void __launch_bounds__(128) tri_twist_solve_kernel(SpecPlan S, double2* __restrict__ spec) {
+  tri_twist_body<AXIS, PACKED>(S, spec, S.sing_cm, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
 // Batched passes: persistent CTAs walk (subdomain, block) work items; the
 // subdomain's arguments are staged in shared memory once per item.
-// PASS: 0 x forward, 1 x inverse, 2 y forward, 3 y inverse, 4 tridiagonal z (packed x).
+// PASS: 0 x forward, 1 x inverse, 2 y forward, 3 y inverse, 4 tridiagonal z (packed x,
+// the twisted solve from the subdomain's table).
 // A subdomain whose plan sets dct_x / dct_y (an axis of 24, 32, 48 or 64
 // points, pressure code 2 or 3) takes the FFT-based line bodies of
 // ns_fft_core.cuh there, with 128 / R1 lines per item so that all 128
@@ -727,7 +859,7 @@ __global__ void __launch_bounds__(128) spec_batch_kernel(const BatchSpecArgs* __
     if (PASS == 1) dense_x_inv_body(a.S, a.spec, a.dp, a.L, sm_b, w.bx);
     if (PASS == 2) dense_yz_body<1, true>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx);
     if (PASS == 3) dense_yz_body<1, false>(a.S, a.spec, reinterpret_cast<double2*>(sm_b), w.bx);
-    if (PASS == 4) tri_lines_body(a.S, a.spec, sm_b, w.bx);
+    if (PASS == 4) tri_twist_body<2, true>(a.S, a.spec, sm_b, w.bx);
     __syncthreads();
   }
 }
@@ -787,7 +919,7 @@ void spec_pass_grid(int pass, const SpecPlan& S, int& gx, int& gy) {
     gx = (S.ny * S.nz + per - 1) / per;
   }
   else if (pass == 2 || pass == 3) gx = (S.nxs * S.nz + 15) / 16;  // dense_yz_body: 16 lines per item
-  else gx = (S.nxs * S.ny + 127) / 128;  // tri_lines_body: 128 lines per item
+  else gx = (S.nxs * S.ny + 63) / 64;  // tri_twist_body: 64 lines per item
 }
 
 size_t spec_pass_smem(int pass, const SpecPlan& S) {
@@ -885,34 +1017,35 @@ cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec
   return cudaGetLastError();
 }
 
-cudaError_t launch_tri_table(int axis, const SpecPlan& S, double2* tab, cudaStream_t st) {
-  const int n_other = axis == 1 ? S.nz : S.ny;
+
+
+cudaError_t launch_tri_twist_table(int axis, const SpecPlan& S, double2* tab, cudaStream_t st) {
   const bool packed = S.kind[0] != 0;
-  const int nreg = packed ? S.nxs : S.nxs - 1;
-  const int nblk = (nreg + TRI_T - 1) / TRI_T;
-  dim3 grid(nblk + (packed ? 0 : 1), n_other);
+  const int nlines = S.nxs * (axis == 1 ? S.nz : S.ny);
+  const int grid = (nlines + 127) / 128;
   if (axis == 1) {
-    if (packed) tri_table_kernel<1, true><<<grid, TRI_T, 0, st>>>(S, tab);
-    else tri_table_kernel<1, false><<<grid, TRI_T, 0, st>>>(S, tab);
+    if (packed) tri_twist_table_kernel<1, true><<<grid, 128, 0, st>>>(S, tab);
+    else tri_twist_table_kernel<1, false><<<grid, 128, 0, st>>>(S, tab);
   } else {
-    if (packed) tri_table_kernel<2, true><<<grid, TRI_T, 0, st>>>(S, tab);
-    else tri_table_kernel<2, false><<<grid, TRI_T, 0, st>>>(S, tab);
+    if (packed) tri_twist_table_kernel<2, true><<<grid, 128, 0, st>>>(S, tab);
+    else tri_twist_table_kernel<2, false><<<grid, 128, 0, st>>>(S, tab);
   }
   return cudaGetLastError();
-}
-
-// The session's table-driven z solve of a packed-x box: 128 lines per CTA,
-// no shared memory (the singular line's multipliers go to S.sing_cm).
-__global__ void __launch_bounds__(128) tri_lines_kernel(SpecPlan S, double2* __restrict__ spec) {
-  tri_lines_body(S, spec, S.sing_cm, blockIdx.x);
 }
 
 cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st) {
   const int N = axis == 1 ? S.ny : S.nz;
   const int n_other = axis == 1 ? S.nz : S.ny;
   const bool packed = S.kind[0] != 0;
-  if (axis == 2 && packed && S.tri_m && S.sing_cm) {
-    tri_lines_kernel<<<(S.nxs * S.ny + 127) / 128, 128, 0, st>>>(S, spec);
+  if (S.tri_tw && S.tri_m && S.sing_cm) {
+    const int grid = (S.nxs * n_other + 63) / 64;
+    if (axis == 1) {
+      if (packed) tri_twist_solve_kernel<1, true><<<grid, 128, 0, st>>>(S, spec);
+      else tri_twist_solve_kernel<1, false><<<grid, 128, 0, st>>>(S, spec);
+    } else {
+      if (packed) tri_twist_solve_kernel<2, true><<<grid, 128, 0, st>>>(S, spec);
+      else tri_twist_solve_kernel<2, false><<<grid, 128, 0, st>>>(S, spec);
+    }
     return cudaGetLastError();
   }
   const size_t sm = (size_t)N * TRI_T * sizeof(double) * (packed ? 2 : 1);

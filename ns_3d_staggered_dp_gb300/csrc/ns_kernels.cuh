@@ -243,10 +243,11 @@ struct FftPlan {
   double tri_h2;          // h_s^2
   double tri_rs;          // h_s^2 * scale of the unnormalised FFT passes
   double tri_elo, tri_ehi;  // end-row diagonal changes: pbc 2 -1, pbc 3 +1, pbc 4 0
-  const double2* tri_m;   // the forward multipliers (re, im) of every line, laid out like the spectrum
-                          // (launch_tri_table); read by the table-driven z solve (tri_lines_body)
-  double* sing_cm;        // session z solve from the table: global scratch (2 nz TRI_T doubles) of the
+  const double2* tri_m;   // the twisted factorisation's multipliers (re, im) of every line, laid out
+                          // like the spectrum (launch_tri_twist_table)
+  double* sing_cm;        // session solve from a table: global scratch (2 N TRI_T doubles) of the
                           // singular line's multipliers (the batch keeps them in shared memory)
+  int tri_tw;             // 1: tri_m holds the twisted multipliers, solved two lanes per line
   // All-periodic boxes: the z stage as cyclic tridiagonal line solves (ns_cyclic.cu)
   // instead of z FFT * 1/lambda * z IFFT.  Tables per (kx, ky) mode, laid out like the
   // spectrum: T's multipliers, w = rs T^-1 e0, q = T^-1 u; per mode (1/c, SM denominator).
@@ -357,10 +358,10 @@ cudaError_t launch_dense_x(bool fwd, const SpecPlan& S, const DivArgs& d, double
 cudaError_t launch_dense_yz(int axis, bool fwd, const SpecPlan& S, double2* spec, cudaStream_t st);
 // Tridiagonal solve of every spectrum line along axis 1 (y) or 2 (z) (ns_dct.cu).
 cudaError_t launch_tri_solve(int axis, const SpecPlan& S, double2* spec, cudaStream_t st);
-// The multipliers of those lines (they depend on the mode and the matrix, not
-// on the data), computed by the solve's own recurrence into tab (one double2
-// per spectrum entry); then set S.tri_m = tab.
-cudaError_t launch_tri_table(int axis, const SpecPlan& S, double2* tab, cudaStream_t st);
+// The twisted factorisation's multipliers of every line along axis 1 or 2,
+// laid out like the spectrum: top-down m_j above the middle row k = N/2,
+// bottom-up n_j below it, the middle pivot at k (ns_dct.cu).
+cudaError_t launch_tri_twist_table(int axis, const SpecPlan& S, double2* tab, cudaStream_t st);
 // Batched spectral passes of all-wall boxes (x dense packed, y dense, z line solve).
 struct BatchSpecArgs {
   SpecPlan S;

@@ -39,7 +39,7 @@ struct ns_handle {
   std::vector<cudaEvent_t> ev_slab;            // ns_step_host: one event per z-slab
   double* inv_lam = nullptr;
   double* cyc_buf = nullptr;  // tables of the cyclic z solve (all-periodic boxes)
-  double2* tri_tab = nullptr;  // z-solve multipliers of a packed-x (all-wall) box
+  double2* tri_tab = nullptr;  // the wall-axis line solve's twisted multipliers (one per spectrum entry)
   double* sing_cm = nullptr;   // its singular line's scratch
   double2* tw = nullptr;  // twiddle tables (x, xr, y, z)
   ns::FftPlan plan{};
