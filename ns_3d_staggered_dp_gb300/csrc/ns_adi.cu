@@ -285,16 +285,52 @@ __global__ void __launch_bounds__(kAdiBatchLines) adi_batch_kernel(const BatchAd
     const int m = S.hi - S.lo + 1;
     const double r_lo = A.face_lo[AXIS][fld] ? __ldg(A.face_lo[AXIS][fld] + tl) : 0.0;
     const double r_hi = A.face_hi[AXIS][fld] ? __ldg(A.face_hi[AXIS][fld] + tl) : 0.0;
+    // the right-hand sides PD unknowns ahead in registers, so no load waits
+    // behind the store to the same line (same operations, same bits)
+    constexpr int PD = 8;
+    auto rhs = [&](int e) -> double {
+      if (e < 0 || e >= m) return 0.0;
+      if (e == 0) return r_lo;
+      if (e == m - 1) return r_hi;
+      return xl[(long long)e * st];
+    };
+    double rb[PD];
+#pragma unroll
+    for (int q = 0; q < PD; ++q) rb[q] = rhs(q);
     double yp = 0.0;
-    for (int e = 0; e < m; ++e) {
-      const double r = e == 0 ? r_lo : (e == m - 1 ? r_hi : xl[(long long)e * st]);
-      yp = fma(-__ldg(lf + e), yp, r);
-      xl[(long long)e * st] = yp;
+    for (int g = 0; g < m; g += PD) {
+      double nb[PD];
+#pragma unroll
+      for (int q = 0; q < PD; ++q) nb[q] = rhs(g + PD + q);
+#pragma unroll
+      for (int q = 0; q < PD; ++q) {
+        const int e = g + q;
+        if (e < m) {
+          yp = fma(-__ldg(lf + e), yp, rb[q]);
+          xl[(long long)e * st] = yp;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < PD; ++q) rb[q] = nb[q];
     }
+    auto yv = [&](int e) -> double { return e >= 0 ? xl[(long long)e * st] : 0.0; };
+#pragma unroll
+    for (int q = 0; q < PD; ++q) rb[q] = yv(m - 1 - q);
     double xn = 0.0;
-    for (int e = m - 1; e >= 0; --e) {
-      xn = fma(-__ldg(cu + e), xn, xl[(long long)e * st] * __ldg(di + e));
-      xl[(long long)e * st] = xn;
+    for (int g = m - 1; g >= 0; g -= PD) {
+      double nb[PD];
+#pragma unroll
+      for (int q = 0; q < PD; ++q) nb[q] = yv(g - PD - q);
+#pragma unroll
+      for (int q = 0; q < PD; ++q) {
+        const int e = g - q;
+        if (e >= 0) {
+          xn = fma(-__ldg(cu + e), xn, rb[q] * __ldg(di + e));
+          xl[(long long)e * st] = xn;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < PD; ++q) rb[q] = nb[q];
     }
   }
 }
