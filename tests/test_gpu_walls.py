@@ -68,6 +68,11 @@ POISSON_CASES = [
     ((512, 16, 24), (2, 3, 3)),
     ((128, 32, 16), (3, 2, 2)),
     ((256, 12, 10), (2, 4, 3)),
+    # the twisted line solve: an odd solve axis (singular, periodic x), a long Neumann solve axis
+    # whose singular line's warp segments do not divide evenly, and a short one on the one-lane path
+    ((32, 16, 21), (1, 3, 3)),
+    ((16, 16, 200), (3, 3, 3)),
+    ((16, 24, 7), (3, 3, 3)),
 ]
 
 
