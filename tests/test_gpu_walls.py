@@ -181,6 +181,19 @@ def test_step_all_wall_box_with_a_long_dense_y():
     _run_compare(cfg, st, 4, faces=faces, cn_faces=cn_faces, div_free=False)
 
 
+@pytest.mark.parametrize("pbc", [3, 2])
+def test_step_all_wall_box_fft_transforms(pbc):
+    """An all-wall box whose x and y transforms go through FFTs (x 64 points,
+    y 48 through the 12-point DFT) and whose z axis takes the twisted line
+    solve: AB2-CN steps with wall faces against the oracle."""
+    cfg = O.Config(64, 48, 32, lx=1.0, ly=0.75, lz=0.5, nu=0.01, dt=1e-3, scheme=O.AB2_CN, bc=(2, 2, 2),
+                   pbc=(pbc,) * 3, dp_flag=1, mean_dp=0.02 if pbc == 3 else 0.0)
+    faces = random_faces(cfg, 31, amp=0.1)
+    cn_faces = [random_faces(cfg, 32 + d, amp=0.1) for d in range(3)]
+    st = random_state(cfg, 33, amp=0.2)
+    _run_compare(cfg, st, 4, faces=faces, cn_faces=cn_faces, div_free=False)
+
+
 @pytest.mark.parametrize("bc,pbc", [((4, 2, 4), (4, 2, 4)), ((2, 4, 2), (2, 3, 2)), ((2, 2, 4), (3, 2, 4))])
 def test_step_wall_codes(bc, pbc):
     """Dirichlet-on-the-ghost (4) and Dirichlet-on-the-wall (2) codes mixed,
