@@ -421,9 +421,10 @@ cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t
   return e;
 }
 
-// The divergence (plus the pressure-BC terms) of the rows, one thread per
-// point, into out[N row + i]: a streaming pass at full occupancy, so the
-// transform reads whole rows instead of six shifted velocity loads.
+// The divergence (plus the pressure-BC terms) of the rows, or the given
+// right-hand side d.rhs, one thread per point, into out[N row + i]: a
+// streaming pass at full occupancy, so the transform reads whole rows
+// instead of six shifted velocity loads.
 template <int N>
 __global__ void __launch_bounds__(256) dct_x_div_kernel(FftPlan P, DivArgs d, double* __restrict__ out, FOne c) {
   const long long idx = blockIdx.x * 256LL + threadIdx.x;
@@ -432,6 +433,10 @@ __global__ void __launch_bounds__(256) dct_x_div_kernel(FftPlan P, DivArgs d, do
   const int j = 1 + row % P.ny, k = 1 + row / P.ny;
   const Layout& L = d.L;
   const long long g = L.at(i + 1, j, k);
+  if (d.rhs) {  // a given right-hand side, already BC-modified
+    out[idx] = d.rhs[g];
+    return;
+  }
   double v = fmul(c, fsub(c, d.us[g + 1], d.us[g]), d.cdx);
   v = fma(fsub(c, d.vs[g + L.sy], d.vs[g]), d.cdy, v);
   v = fma(fsub(c, d.ws[g + L.sz], d.ws[g]), d.cdz, v);
@@ -479,7 +484,7 @@ cudaError_t launch_dct_x_n(bool fwd, const FftPlan& P, const DivArgs* d, double2
 }
 
 cudaError_t launch_dct_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st, const Marker& mk) {
-  if ((P.dct_x != 2 && P.dct_x != 3) || d.rhs) return cudaErrorInvalidValue;
+  if (P.dct_x != 2 && P.dct_x != 3) return cudaErrorInvalidValue;
   cudaError_t e = cudaSuccess;
 #define DCT_XF(n)                                                                                   \
   e = P.dct_x == 2 ? launch_dct_x_n<(n), 2>(true, P, &d, spec, nullptr, nullptr, d.L, st, &mk)      \
@@ -544,7 +549,7 @@ cudaError_t launch_poisson_fwd(const FftPlan& P, const DivArgs& d, double2* spec
 #undef X_FWD
     if (e != cudaSuccess) return e;
     mk("fft_x_fwd");
-  } else if (P.dct_x && !d.rhs) {
+  } else if (P.dct_x) {
     if ((e = launch_dct_x_fwd(P, d, spec, st, mk)) != cudaSuccess) return e;
     mk("dct_x_fwd");
   } else {

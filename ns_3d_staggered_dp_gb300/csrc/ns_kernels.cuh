@@ -297,7 +297,8 @@ using SpecPlan = FftPlan;
 cudaError_t launch_dct_y(bool fwd, const FftPlan& P, double2* spec, cudaStream_t st);
 struct DivArgs;
 // The FFT-based x transforms of a plan with dct_x set (ns_fft.cu): divergence
-// (+ pressure-BC terms) -> packed modes, and packed modes -> dp slots 1..nx.
+// (+ pressure-BC terms), or d.rhs when given, -> packed modes, and packed
+// modes -> dp slots 1..nx.
 cudaError_t launch_dct_x_fwd(const FftPlan& P, const DivArgs& d, double2* spec, cudaStream_t st, const Marker& mk);
 cudaError_t launch_dct_x_inv(const FftPlan& P, const double2* spec, double* dp, const Layout& L, cudaStream_t st);
 struct DivArgs {
