@@ -6,11 +6,17 @@ pr_bc_staggered :1403-1464), its mix with periodic FFT axes, and full steps
 with wall velocity BCs (vel_bc_staggered :213-310, the banded CN-ADI of
 re_simulation_sub_tstep_interBC_combine.f90:656-701 with per-sweep faces).
 
-Tolerances: the dense trigonometric transforms and the tridiagonal line
-solves round differently from the
-oracle's scipy DCT/DST, and the wall Poisson problem is less well
-conditioned than the periodic one, so the routine bound is a relative L2 of
-1e-11; full steps keep the 1e-10 per-field bound and max|div u| <= 1e-12.
+The wall axes are transformed through FFTs (Makhoul DCT-II/III: 24, 48 and
+powers of two from 32 to 512 cells, codes 2 and 3) or by exact dense pairs
+(the other sizes and code 4); the last wall axis is solved line by line
+(the twisted factorisation from a multiplier table, the singular line by a
+warp; the one-lane Thomas solve below 8 rows).  The cases cover each.
+
+Tolerances: the trigonometric transforms and the tridiagonal line solves
+round differently from the oracle's scipy DCT/DST, and the wall Poisson
+problem is less well conditioned than the periodic one, so the routine bound
+is a relative L2 of 1e-11; full steps keep the 1e-10 per-field bound and
+max|div u| <= 1e-12.
 """
 import numpy as np
 import pytest
