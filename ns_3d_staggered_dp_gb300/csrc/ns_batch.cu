@@ -393,9 +393,10 @@ struct ns_batch {
   struct Range { long long off = 0; int cnt = 0; int cnt_dense = 0; };
   std::vector<std::vector<Range>> rng;                  // [set][stage]
   std::vector<std::vector<std::vector<Range>>> sub_rng; // [set][stage][sub]
-  // the divergence items of the x forward stage (subdomains with an FFT-based x)
-  std::vector<Range> div_rng;                           // [set]
-  std::vector<std::vector<Range>> sub_div_rng;          // [set][sub]
+  // the divergence items of the x forward stage (subdomains with an FFT-based
+  // x), and those of their boundary cells' pressure-BC terms
+  std::vector<Range> div_rng, bc_rng;                   // [set]
+  std::vector<std::vector<Range>> sub_div_rng, sub_bc_rng;  // [set][sub]
   std::vector<std::vector<int>> active;                 // [set] -> subdomains
   size_t spec_smem[5] = {0, 0, 0, 0, 0};
   size_t spec_smem_dct[4] = {0, 0, 0, 0};
@@ -484,6 +485,12 @@ cudaError_t launch_stage_kernel(ns_batch* b, int set, int stage, bool first, cud
           const ns_batch::Range& dr = loop ? b->sub_div_rng[set][act[k]] : b->div_rng[set];
           if (dr.cnt > 0) {
             e = launch_spec_batch_div(b->d_spec[v], b->d_items + dr.off, dr.cnt, 0, st);
+            if (e != cudaSuccess) return e;
+            ++b->launches;
+          }
+          const ns_batch::Range& br = loop ? b->sub_bc_rng[set][act[k]] : b->bc_rng[set];
+          if (br.cnt > 0) {
+            e = launch_spec_batch_bc(b->d_spec[v], b->d_items + br.off, br.cnt, 0, st);
             if (e != cudaSuccess) return e;
             ++b->launches;
           }
@@ -1064,6 +1071,20 @@ int ns_batch_create(const ns_batch_config* cfg, const ns_subdomain* subs, int n,
       for (int q = 0; q < nq; ++q) all.push_back(BatchItem{i, q, 0, 0});
     }
     b->div_rng[set].cnt = (int)((long long)all.size() - b->div_rng[set].off);
+  }
+  b->bc_rng.assign(nsets, ns_batch::Range{});
+  b->sub_bc_rng.assign(nsets, std::vector<ns_batch::Range>(n));
+  for (int set = 0; set < nsets; ++set) {
+    b->bc_rng[set].off = (long long)all.size();
+    for (int i : b->active[set]) {
+      if (!stage_dct(ST_XF, i) || !b->plan[i].any_bc_term()) continue;
+      const long long nbc = b->plan[i].bc_cells();
+      const int nq = (int)((nbc + kDivChunk - 1) / kDivChunk);
+      b->sub_bc_rng[set][i].off = (long long)all.size();
+      b->sub_bc_rng[set][i].cnt = nq;
+      for (int q = 0; q < nq; ++q) all.push_back(BatchItem{i, q, 0, 0});
+    }
+    b->bc_rng[set].cnt = (int)((long long)all.size() - b->bc_rng[set].off);
   }
   b->gather_rng.off = (long long)all.size();
   for (int i = 0; i < n; ++i) {

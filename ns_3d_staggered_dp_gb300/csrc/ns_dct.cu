@@ -885,9 +885,48 @@ __global__ void __launch_bounds__(kDivChunk) spec_batch_div_kernel(const BatchSp
     if (e < N * (unsigned)a.S.ny * (unsigned)a.S.nz) {
       const int row = (int)(e / N), i = (int)(e - (unsigned)row * N);
       const FOne c{a.d.one, a.d.mzero};
-      reinterpret_cast<double*>(a.spec)[e] = rhs_cell(a.d, a.S, c, i + 1, 1 + row % a.S.ny, 1 + row / a.S.ny);
+      const DivArgs& d = a.d;
+      double v;
+      if (d.rhs) {
+        v = d.rhs[d.L.at(i + 1, 1 + row % a.S.ny, 1 + row / a.S.ny)];
+      } else {  // the divergence; the boundary cells' terms follow in spec_batch_bc_kernel
+        const long long g = d.L.at(i + 1, 1 + row % a.S.ny, 1 + row / a.S.ny);
+        v = fmul(c, fsub(c, d.us[g + 1], d.us[g]), d.cdx);
+        v = fma(fsub(c, d.vs[g + d.L.sy], d.vs[g]), d.cdy, v);
+        v = fma(fsub(c, d.ws[g + d.L.sz], d.ws[g]), d.cdz, v);
+        v = v + 0.0;
+      }
+      reinterpret_cast<double*>(a.spec)[e] = v;
     }
   }
+}
+
+// The pressure-BC terms of those subdomains' boundary cells, added to their
+// divergence rows (item (sub, q): boundary cells [kDivChunk q, kDivChunk (q+1))
+// in the order of SpecPlan::bc_cell).
+__global__ void __launch_bounds__(kDivChunk) spec_batch_bc_kernel(const BatchSpecArgs* __restrict__ tab,
+                                                                  const BatchItem* __restrict__ items, int n_items) {
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    const BatchSpecArgs& a = tab[w.sub];
+    const long long q = (long long)w.bx * kDivChunk + threadIdx.x;
+    if (q < a.S.bc_cells()) {
+      int i, j, k;
+      a.S.bc_cell(q, i, j, k);
+      double* out = reinterpret_cast<double*>(a.spec);
+      const long long e = (long long)a.S.nx * ((j - 1) + (long long)a.S.ny * (k - 1)) + (i - 1);
+      out[e] = out[e] + a.S.bc_term_edge(i, j, k);
+    }
+  }
+}
+
+cudaError_t launch_spec_batch_bc(const BatchSpecArgs* tab, const BatchItem* items, int n_items, int grid,
+                                 cudaStream_t st) {
+  if (n_items <= 0) return cudaSuccess;
+  if (grid <= 0) grid = 8 * 152;
+  if (grid > n_items) grid = n_items;
+  spec_batch_bc_kernel<<<grid, kDivChunk, 0, st>>>(tab, items, n_items);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_spec_batch_div(const BatchSpecArgs* tab, const BatchItem* items, int n_items, int grid,

@@ -440,7 +440,20 @@ __global__ void __launch_bounds__(256) dct_x_div_kernel(FftPlan P, DivArgs d, do
   double v = fmul(c, fsub(c, d.us[g + 1], d.us[g]), d.cdx);
   v = fma(fsub(c, d.vs[g + L.sy], d.vs[g]), d.cdy, v);
   v = fma(fsub(c, d.ws[g + L.sz], d.ws[g]), d.cdz, v);
-  out[idx] = v + P.bc_term(i + 1, j, k);
+  out[idx] = v + 0.0;  // the boundary cells' terms follow in dct_x_bc_kernel
+}
+
+// The pressure-BC terms of the boundary cells (pr_bc_staggered_modify_rhs,
+// NS_functions.f90:1345-1400) added to the divergence rows: a pass over the
+// boundary cells only, so that the divergence kernel's warps do not branch
+// at every row's ends.
+__global__ void __launch_bounds__(256) dct_x_bc_kernel(FftPlan P, double* __restrict__ out) {
+  const long long q = blockIdx.x * 256LL + threadIdx.x;
+  if (q >= P.bc_cells()) return;
+  int i, j, k;
+  P.bc_cell(q, i, j, k);
+  const long long e = (long long)P.nx * ((j - 1) + (long long)P.ny * (k - 1)) + (i - 1);
+  out[e] = out[e] + P.bc_term_edge(i, j, k);
 }
 
 // The session's FFT-based x transforms (dct_x_fwd_body in place on the
@@ -471,6 +484,10 @@ cudaError_t launch_dct_x_n(bool fwd, const FftPlan& P, const DivArgs* d, double2
     const long long pts = (long long)N * P.ny * P.nz;
     dct_x_div_kernel<N><<<(unsigned)((pts + 255) / 256), 256, 0, st>>>(P, *d, reinterpret_cast<double*>(spec), c);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (!d->rhs && P.any_bc_term()) {
+      dct_x_bc_kernel<<<(unsigned)((P.bc_cells() + 255) / 256), 256, 0, st>>>(P, reinterpret_cast<double*>(spec));
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     if (mk) (*mk)("dct_x_div");
     e = cudaFuncSetAttribute(dct_x_fwd_kernel<N, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;

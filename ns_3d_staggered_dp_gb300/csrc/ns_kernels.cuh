@@ -287,6 +287,32 @@ struct FftPlan {
     }
     return t;
   }
+  // The boundary cells of the interior box, each once: the x faces (i = 1,
+  // nx; every j, k), then the y faces (j = 1, ny; 1 < i < nx; every k), then
+  // the z faces (k = 1, nz; 1 < i < nx, 1 < j < ny).  A pass over them adds
+  // bc_term_edge to a divergence computed without it: (div + 0) + t is
+  // div + t bit for bit (t starts at +0 and only gains products, so it is
+  // never -0).
+  __host__ __device__ long long bc_cells() const {
+    return 2LL * ny * nz + 2LL * (nx - 2) * nz + 2LL * (nx - 2) * (ny - 2);
+  }
+  __device__ __forceinline__ void bc_cell(long long q, int& i, int& j, int& k) const {
+    const long long fx = (long long)ny * nz, fy = (long long)(nx - 2) * nz;
+    if (q < 2 * fx) {
+      const long long r = q % fx;
+      i = q < fx ? 1 : nx; j = 1 + (int)(r % ny); k = 1 + (int)(r / ny);
+      return;
+    }
+    q -= 2 * fx;
+    if (q < 2 * fy) {
+      const long long r = q % fy;
+      j = q < fy ? 1 : ny; i = 2 + (int)(r % (nx - 2)); k = 1 + (int)(r / (nx - 2));
+      return;
+    }
+    q -= 2 * fy;
+    const long long fz = (long long)(nx - 2) * (ny - 2), r = q % fz;
+    k = q < fz ? 1 : nz; i = 2 + (int)(r % (nx - 2)); j = 2 + (int)(r / (nx - 2));
+  }
   __host__ __device__ bool any_bc_term() const {
     return mod_lo[0] != 0.0 || mod_hi[0] != 0.0 || mod_lo[1] != 0.0 || mod_hi[1] != 0.0 || mod_lo[2] != 0.0 ||
            mod_hi[2] != 0.0;
@@ -388,6 +414,10 @@ cudaError_t launch_spec_batch(int pass, bool dct, const BatchSpecArgs* tab, cons
 constexpr int kDivChunk = 256;
 cudaError_t launch_spec_batch_div(const BatchSpecArgs* tab, const BatchItem* items, int n_items, int grid,
                                   cudaStream_t st);
+// Then the pressure-BC terms of their boundary cells (SpecPlan::bc_cell
+// order; item (sub, q) covers cells [kDivChunk q, kDivChunk (q+1))).
+cudaError_t launch_spec_batch_bc(const BatchSpecArgs* tab, const BatchItem* items, int n_items, int grid,
+                                 cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Correction (ns_correct.cu)
